@@ -1,0 +1,190 @@
+/* LolaCUDA — GB300 (sm_103a) cone-beam backprojection module for RabbitCT.
+ *
+ * C ABI of liblolacuda.so.  Three groups of entry points:
+ *
+ *  1. The RabbitCT module API.  lolaCudaPrepare / lolaCudaBackprojection /
+ *     lolaCudaFinish have exactly the signatures of the reference's module
+ *     function-pointer types (HPC-Dwarfs/RabbitCT src/moduleLoader_types.h:10-12)
+ *     and are registered as one more row of the static algorithm table
+ *     (src/algorithmRegistry.c:39-48), so the stock rabbitRunner drives them
+ *     like LolaBunny / LolaOPT / LolaASM.
+ *
+ *  2. Configuration (no counterpart in the reference, whose modules are
+ *     configured at compile time): storage type of the projections, the
+ *     accumulation mode, the number of projections staged per kernel pass and
+ *     the error convention.
+ *
+ *  3. The plan API: the same kernels driven on device-resident data, for
+ *     callers that keep projections in HBM (the benchmark, batched
+ *     reconstructions, tests).  All pointers named d_* are device pointers.
+ *
+ * Return convention: 1 = success, 0 = failure (message in lolaCudaLastError()),
+ * like the reference modules' `return 1`.  By default the three module entry
+ * points print the error and exit(EXIT_FAILURE) on failure, which is the
+ * reference convention (src/error.h:21-31) and necessary because rabbitRunner
+ * ignores the return codes (src/rabbitRunner.c:225,279,287).
+ */
+#ifndef LOLACUDA_H
+#define LOLACUDA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- RabbitCT data contract --------------------------------------------
+ * Layout-identical to the reference's src/rabbitCt.h:9-27.  The include guard
+ * of that header is honoured in both directions so the two headers can be
+ * included together in a registry translation unit. */
+#ifndef RABBITRUNNER_TYPES_H
+#define RABBITRUNNER_TYPES_H
+typedef struct {
+  int id;          /* 1-based global projection index */
+  double *matrix;  /* 12 doubles, 3x4 column-major: a[col*3 + row] */
+  float *image;    /* imageWidth * imageHeight floats, image[j*W + i] */
+} Projection;
+
+typedef struct {
+  uint32_t problemSize;          /* N: volume is N^3 voxels */
+  uint32_t imageWidth;
+  uint32_t imageHeight;
+  float voxelSize;               /* mm */
+  float O_Index;                 /* world coordinate of voxel index 0 */
+  float *volumeData;             /* N^3 floats, x fastest, host */
+  uint32_t numberOfProjections;  /* total at prepare with -a, else 0; per call: batch size */
+  double *globalGeometry;        /* numberOfProjections * 12 doubles (with -a) */
+  Projection *projectionBuffer;
+  char *clipFilename;
+} RabbitCtGlobalData;
+#endif
+
+/* ---- 1. Module API --------------------------------------------------------
+ * Replaces FncPrepareAlgorithmType (src/moduleLoader_types.h:10).  Called once
+ * (src/rabbitRunner.c:222-232).  Allocates the device volume and the
+ * projection ring and uploads the caller's volumeData as the starting volume. */
+int lolaCudaPrepare(RabbitCtGlobalData *data);
+
+/* Replaces FncAlgorithmIterationType (src/moduleLoader_types.h:11).  Called
+ * once per batch of data->numberOfProjections projections
+ * (src/rabbitRunner.c:279).  The projections' images and matrices are copied
+ * before it returns (the runner overwrites them, src/rabbitRunner.c:275-278).
+ * Projections are staged until `batch` are buffered or the last global id is
+ * reached, then backprojected; with syncEachCall (default) the call returns
+ * only after that work finished, so the runner's timer covers it. */
+int lolaCudaBackprojection(RabbitCtGlobalData *data);
+
+/* Replaces FncFinishAlgorithmType (src/moduleLoader_types.h:12).  Flushes any
+ * staged projections, copies the volume to data->volumeData and frees all
+ * device resources (src/rabbitRunner.c:287). */
+int lolaCudaFinish(RabbitCtGlobalData *data);
+
+/* ---- 2. Configuration ------------------------------------------------------ */
+#define LOLA_MAX_BATCH 32
+
+enum {
+  LOLA_STORE_F32 = 0,   /* 4 FP32 taps per update */
+  LOLA_STORE_F16 = 1,   /* 4 FP16 taps */
+  LOLA_STORE_BF16 = 2,  /* 4 BF16 taps */
+  LOLA_STORE_F32Q = 3,  /* FP32, 2x2 neighbourhood packed per pixel: 1 x 16 B load */
+  LOLA_STORE_F16Q = 4,  /* FP16, packed 2x2: 1 x 8 B load */
+  LOLA_STORE_BF16Q = 5  /* BF16, packed 2x2: 1 x 8 B load */
+};
+
+enum {
+  LOLA_ACCUM_PLAIN = 0, /* vol += term, FP32 */
+  LOLA_ACCUM_KAHAN = 1  /* compensated FP32 summation over each kernel pass */
+};
+
+typedef struct {
+  int32_t storage;       /* LOLA_STORE_* */
+  int32_t accumulation;  /* LOLA_ACCUM_* */
+  int32_t batch;         /* projections per kernel pass, 1..LOLA_MAX_BATCH */
+  int32_t voxelsPerThread; /* voxels per thread along z: 4, 8 or 16 (0 = default) */
+  int32_t rowsPerBlock;  /* warps (y rows) per block: 4 or 8 (0 = default) */
+  int32_t syncEachCall;  /* module API: wait for the pass before returning */
+  int32_t exitOnError;   /* module API: print + exit(EXIT_FAILURE) on error */
+  int32_t collectStats;  /* record CUDA events around every backprojection pass */
+  int32_t device;        /* CUDA device ordinal */
+  int32_t reserved[7];
+} LolaCudaConfig;
+
+/* Defaults: FP32 storage, plain accumulation, batch 16, 8 voxels per thread,
+ * 8 rows per block, syncEachCall 1, exitOnError 1, no stats, device 0.
+ * Environment overrides read by lolaCudaDefaultConfig: LOLACUDA_STORAGE
+ * (f32|f16|bf16|f32q|f16q|bf16q), LOLACUDA_ACCUM (plain|kahan),
+ * LOLACUDA_BATCH, LOLACUDA_VPT, LOLACUDA_ROWS, LOLACUDA_SYNC, LOLACUDA_EXIT. */
+void lolaCudaDefaultConfig(LolaCudaConfig *config);
+
+/* Configuration used by the next lolaCudaPrepare (module API). */
+int lolaCudaSetConfig(const LolaCudaConfig *config);
+int lolaCudaGetConfig(LolaCudaConfig *config);
+
+/* Last error message of this thread ("" if none). */
+const char *lolaCudaLastError(void);
+
+/* ---- 3. Plan API ------------------------------------------------------------ */
+typedef struct {
+  int32_t problemSize;   /* N */
+  int32_t imageWidth;
+  int32_t imageHeight;
+  float voxelSize;
+  float originIndex;     /* O_Index */
+} LolaCudaGeometry;
+
+typedef struct {
+  int64_t passes;        /* backprojection kernel launches since the last reset */
+  int64_t packs;         /* projection-conversion kernel launches */
+  int64_t projections;   /* projections backprojected */
+  double passMs;         /* summed CUDA-event time of the passes (collectStats) */
+  int64_t tilePassesFast;  /* (tile, projection) pairs on the unclamped path */
+  int64_t tilePassesSlow;  /* ... on the clamped border path */
+  int64_t tilePassesSkipped; /* ... whose footprint misses the detector */
+} LolaCudaStats;
+
+typedef struct LolaCudaPlan LolaCudaPlan;
+
+/* Allocates the device volume (zeroed) and the projection ring. */
+int lolaCudaPlanCreate(const LolaCudaGeometry *geometry, const LolaCudaConfig *config,
+    LolaCudaPlan **plan);
+int lolaCudaPlanDestroy(LolaCudaPlan *plan);
+
+/* Device pointer of the N^3 FP32 volume (x fastest). */
+float *lolaCudaPlanVolume(LolaCudaPlan *plan);
+/* cudaStream_t the plan launches on. */
+void *lolaCudaPlanStream(LolaCudaPlan *plan);
+
+int lolaCudaPlanZeroVolume(LolaCudaPlan *plan);
+int lolaCudaPlanUploadVolume(LolaCudaPlan *plan, const float *h_volume);
+int lolaCudaPlanDownloadVolume(LolaCudaPlan *plan, float *h_volume);
+
+/* Backprojects `count` FP32 projections that are already in device memory
+ * (d_images[p * imageStride + j * W + i]) with host matrices
+ * h_matrices[p * 12 + ...], in passes of `batch`.  Asynchronous on the plan's
+ * stream; the matrices are consumed before the call returns. */
+int lolaCudaPlanBackprojectDevice(LolaCudaPlan *plan, const float *d_images,
+    size_t imageStride, const double *h_matrices, int count);
+
+/* Same from host images (h_images[p * imageStride + ...]); the images are
+ * copied to the device before the call returns. */
+int lolaCudaPlanBackprojectHost(LolaCudaPlan *plan, const float *h_images,
+    size_t imageStride, const double *h_matrices, int count);
+
+int lolaCudaPlanSynchronize(LolaCudaPlan *plan);
+int lolaCudaPlanGetStats(LolaCudaPlan *plan, LolaCudaStats *stats);
+int lolaCudaPlanResetStats(LolaCudaPlan *plan);
+
+/* Small device-memory helpers so hosts without a CUDA binding (ctypes, cgo)
+ * can stage device-resident inputs. */
+void *lolaCudaDeviceAlloc(size_t bytes);
+int lolaCudaDeviceFree(void *d_ptr);
+int lolaCudaCopyToDevice(void *d_dst, const void *h_src, size_t bytes);
+int lolaCudaCopyToHost(void *h_dst, const void *d_src, size_t bytes);
+int lolaCudaDeviceSynchronize(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* LOLACUDA_H */

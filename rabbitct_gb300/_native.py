@@ -1,0 +1,177 @@
+"""ctypes bindings of liblolacuda.so (include/lolaCuda.h) and librctsynth.so.
+
+The CUDA library must be present: every entry point here raises if it is
+missing instead of falling back to anything else.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+_LIB_DIR = Path(__file__).resolve().parent / "_lib"
+
+
+class LolaCudaError(RuntimeError):
+    pass
+
+
+# ---- RabbitCT data contract (src/rabbitCt.h:9-27 of the reference) ----------
+
+class Projection(C.Structure):
+    _fields_ = [("id", C.c_int),
+                ("matrix", C.POINTER(C.c_double)),
+                ("image", C.POINTER(C.c_float))]
+
+
+class RabbitCtGlobalData(C.Structure):
+    _fields_ = [("problemSize", C.c_uint32),
+                ("imageWidth", C.c_uint32),
+                ("imageHeight", C.c_uint32),
+                ("voxelSize", C.c_float),
+                ("O_Index", C.c_float),
+                ("volumeData", C.POINTER(C.c_float)),
+                ("numberOfProjections", C.c_uint32),
+                ("globalGeometry", C.POINTER(C.c_double)),
+                ("projectionBuffer", C.POINTER(Projection)),
+                ("clipFilename", C.c_char_p)]
+
+
+class LolaCudaConfig(C.Structure):
+    _fields_ = [("storage", C.c_int32),
+                ("accumulation", C.c_int32),
+                ("batch", C.c_int32),
+                ("voxelsPerThread", C.c_int32),
+                ("rowsPerBlock", C.c_int32),
+                ("syncEachCall", C.c_int32),
+                ("exitOnError", C.c_int32),
+                ("collectStats", C.c_int32),
+                ("device", C.c_int32),
+                ("reserved", C.c_int32 * 7)]
+
+
+class LolaCudaGeometry(C.Structure):
+    _fields_ = [("problemSize", C.c_int32),
+                ("imageWidth", C.c_int32),
+                ("imageHeight", C.c_int32),
+                ("voxelSize", C.c_float),
+                ("originIndex", C.c_float)]
+
+
+class LolaCudaStats(C.Structure):
+    _fields_ = [("passes", C.c_int64),
+                ("packs", C.c_int64),
+                ("projections", C.c_int64),
+                ("passMs", C.c_double),
+                ("tilePassesFast", C.c_int64),
+                ("tilePassesSlow", C.c_int64),
+                ("tilePassesSkipped", C.c_int64)]
+
+
+STORAGE = {"f32": 0, "f16": 1, "bf16": 2, "f32q": 3, "f16q": 4, "bf16q": 5}
+ACCUM = {"plain": 0, "kahan": 1}
+MAX_BATCH = 32
+
+# every symbol include/lolaCuda.h declares: (name, restype, argtypes)
+_P = C.c_void_p
+_SIGNATURES = [
+    ("lolaCudaPrepare", C.c_int, [C.POINTER(RabbitCtGlobalData)]),
+    ("lolaCudaBackprojection", C.c_int, [C.POINTER(RabbitCtGlobalData)]),
+    ("lolaCudaFinish", C.c_int, [C.POINTER(RabbitCtGlobalData)]),
+    ("lolaCudaDefaultConfig", None, [C.POINTER(LolaCudaConfig)]),
+    ("lolaCudaSetConfig", C.c_int, [C.POINTER(LolaCudaConfig)]),
+    ("lolaCudaGetConfig", C.c_int, [C.POINTER(LolaCudaConfig)]),
+    ("lolaCudaLastError", C.c_char_p, []),
+    ("lolaCudaPlanCreate", C.c_int, [C.POINTER(LolaCudaGeometry), C.POINTER(LolaCudaConfig),
+                                      C.POINTER(_P)]),
+    ("lolaCudaPlanDestroy", C.c_int, [_P]),
+    ("lolaCudaPlanVolume", _P, [_P]),
+    ("lolaCudaPlanStream", _P, [_P]),
+    ("lolaCudaPlanZeroVolume", C.c_int, [_P]),
+    ("lolaCudaPlanUploadVolume", C.c_int, [_P, _P]),
+    ("lolaCudaPlanDownloadVolume", C.c_int, [_P, _P]),
+    ("lolaCudaPlanBackprojectDevice", C.c_int, [_P, _P, C.c_size_t, _P, C.c_int]),
+    ("lolaCudaPlanBackprojectHost", C.c_int, [_P, _P, C.c_size_t, _P, C.c_int]),
+    ("lolaCudaPlanSynchronize", C.c_int, [_P]),
+    ("lolaCudaPlanGetStats", C.c_int, [_P, C.POINTER(LolaCudaStats)]),
+    ("lolaCudaPlanResetStats", C.c_int, [_P]),
+    ("lolaCudaDeviceAlloc", _P, [C.c_size_t]),
+    ("lolaCudaDeviceFree", C.c_int, [_P]),
+    ("lolaCudaCopyToDevice", C.c_int, [_P, _P, C.c_size_t]),
+    ("lolaCudaCopyToHost", C.c_int, [_P, _P, C.c_size_t]),
+    ("lolaCudaDeviceSynchronize", C.c_int, []),
+]
+
+_lola = None
+_synth = None
+
+
+def lib_path() -> Path:
+    return _LIB_DIR / "liblolacuda.so"
+
+
+def load_lolacuda() -> C.CDLL:
+    """Loads liblolacuda.so; raises if it was not built (no fallback)."""
+    global _lola
+    if _lola is None:
+        path = lib_path()
+        if not path.exists():
+            raise LolaCudaError(f"{path} is missing: build it with "
+                                "`python -c 'import __graft_entry__ as g; g.build()'`")
+        lib = C.CDLL(str(path))
+        for name, res, args in _SIGNATURES:
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lola = lib
+    return _lola
+
+
+def last_error() -> str:
+    msg = load_lolacuda().lolaCudaLastError()
+    return msg.decode() if msg else ""
+
+
+def check(ok: int, what: str) -> None:
+    if not ok:
+        raise LolaCudaError(f"{what}: {last_error()}")
+
+
+def load_synth() -> C.CDLL:
+    global _synth
+    if _synth is None:
+        path = _LIB_DIR / "librctsynth.so"
+        if not path.exists():
+            raise LolaCudaError(f"{path} is missing: run rabbitct_gb300.build.build_all()")
+        lib = C.CDLL(str(path))
+        lib.rctSynthMatrices.restype = None
+        lib.rctSynthMatrices.argtypes = [_P, _P]
+        lib.rctSynthPhantom.restype = C.c_int
+        lib.rctSynthPhantom.argtypes = [C.c_uint64, C.c_int, C.c_double, _P]
+        lib.rctSynthProjections.restype = None
+        lib.rctSynthProjections.argtypes = [_P, _P, C.c_int, C.c_double, C.c_uint64, _P]
+        _synth = lib
+    return _synth
+
+
+def ptr(a: np.ndarray) -> int:
+    assert a.flags["C_CONTIGUOUS"], "array must be C-contiguous"
+    return a.ctypes.data
+
+
+def config(storage: str = "f32", accumulation: str = "plain", batch: int = 16,
+           voxels_per_thread: int = 8, rows_per_block: int = 8, sync_each_call: int = 1,
+           exit_on_error: int = 0, collect_stats: int = 0, device: int = 0) -> LolaCudaConfig:
+    c = LolaCudaConfig()
+    load_lolacuda().lolaCudaDefaultConfig(C.byref(c))
+    c.storage = STORAGE[storage]
+    c.accumulation = ACCUM[accumulation]
+    c.batch = batch
+    c.voxelsPerThread = voxels_per_thread
+    c.rowsPerBlock = rows_per_block
+    c.syncEachCall = sync_each_call
+    c.exitOnError = exit_on_error
+    c.collectStats = collect_stats
+    c.device = device
+    return c

@@ -1,0 +1,123 @@
+"""In-tree build of the native libraries (no cmake, no pip install).
+
+Products (git-ignored, rebuilt on every machine):
+  rabbitct_gb300/_lib/liblolacuda.so   CUDA kernels (sm_103a) + C host code
+  rabbitct_gb300/_lib/librctsynth.so   synthetic scan generator (host C)
+
+The CUDA translation units are compiled in parallel, one per storage layout,
+for ``-gencode arch=compute_103a,code=sm_103a`` only.
+"""
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+from concurrent.futures import ThreadPoolExecutor
+from pathlib import Path
+
+PKG = Path(__file__).resolve().parent
+CSRC = PKG / "csrc"
+LIB = PKG / "_lib"
+OBJ = PKG / "_build"
+REPO = PKG.parent
+INCLUDE = REPO / "include"
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+CU_SOURCES = [
+    "bp_f32.cu", "bp_f16.cu", "bp_bf16.cu", "bp_f32q.cu", "bp_f16q.cu", "bp_bf16q.cu",
+    "lolacuda_dispatch.cu",
+]
+C_SOURCES = ["lolacuda_host.c"]
+
+
+def _cuda_home() -> Path:
+    env = os.environ.get("CUDA_HOME") or os.environ.get("CUDA_PATH")
+    if env:
+        return Path(env)
+    nvcc = shutil.which("nvcc")
+    if nvcc:
+        return Path(nvcc).resolve().parent.parent
+    return Path("/usr/local/cuda")
+
+
+def _run(cmd: list[str]) -> None:
+    proc = subprocess.run(cmd, capture_output=True, text=True)
+    if proc.returncode != 0:
+        raise RuntimeError(f"command failed ({proc.returncode}): {' '.join(cmd)}\n"
+                           f"{proc.stdout}\n{proc.stderr}")
+
+
+def _stale(target: Path, deps: list[Path]) -> bool:
+    if not target.exists():
+        return True
+    t = target.stat().st_mtime
+    return any(d.stat().st_mtime > t for d in deps)
+
+
+def build_synth(force: bool = False) -> Path:
+    LIB.mkdir(exist_ok=True)
+    out = LIB / "librctsynth.so"
+    src = CSRC / "rct_synth.c"
+    if force or _stale(out, [src]):
+        _run(["gcc", "-O2", "-fno-fast-math", "-ffp-contract=off", "-std=c99", "-fopenmp",
+              "-fPIC", "-shared", "-o", str(out), str(src), "-lm"])
+    return out
+
+
+def build_lolacuda(force: bool = False, jobs: int | None = None) -> Path:
+    LIB.mkdir(exist_ok=True)
+    OBJ.mkdir(exist_ok=True)
+    cuda = _cuda_home()
+    nvcc = str(cuda / "bin" / "nvcc")
+    out = LIB / "liblolacuda.so"
+    headers = [CSRC / "bp_kernels.cuh", CSRC / "lolacuda_internal.h", INCLUDE / "lolaCuda.h"]
+    common_inc = ["-I" + str(INCLUDE), "-I" + str(CSRC)]
+
+    def compile_cu(name: str) -> Path:
+        src = CSRC / name
+        obj = OBJ / (name + ".o")
+        if force or _stale(obj, [src] + headers):
+            _run([nvcc, *ARCH, "-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC",
+                  *common_inc, "-c", str(src), "-o", str(obj)])
+        return obj
+
+    def compile_c(name: str) -> Path:
+        src = CSRC / name
+        obj = OBJ / (name + ".o")
+        if force or _stale(obj, [src] + headers):
+            _run(["gcc", "-O2", "-std=c99", "-fPIC", "-Wall", "-Wextra", "-Wno-unused-parameter",
+                  *common_inc, "-I" + str(cuda / "include"), "-c", str(src), "-o", str(obj)])
+        return obj
+
+    with ThreadPoolExecutor(max_workers=jobs or min(8, os.cpu_count() or 4)) as ex:
+        futs = [ex.submit(compile_cu, n) for n in CU_SOURCES]
+        futs += [ex.submit(compile_c, n) for n in C_SOURCES]
+        objs = [f.result() for f in futs]
+    if force or _stale(out, objs):
+        _run([nvcc, *ARCH, "-shared", "-o", str(out), *map(str, objs), "-cudart", "static"])
+    return out
+
+
+def build_oracle(force: bool = False) -> Path:
+    """Builds the oracle (test infrastructure) and, where the reference sources
+    are present, the reference itself into oracle/_ref."""
+    oracle = REPO / "oracle"
+    if force:
+        _run(["make", "-C", str(oracle), "clean"])
+    _run(["make", "-C", str(oracle)])
+    ref = Path(os.environ.get("RABBITCT_REFERENCE", "/root/reference"))
+    if (ref / "src" / "LolaBunny.c").exists():
+        _run(["make", "-C", str(REPO), "-f", "oracle/ref.mk", f"REF={ref}"])
+    return oracle / "liboracle.so"
+
+
+def build_all(force: bool = False) -> None:
+    build_synth(force)
+    build_lolacuda(force)
+    build_oracle(force)
+
+
+if __name__ == "__main__":
+    import sys
+    build_all(force="--force" in sys.argv)
+    print("built", *sorted(p.name for p in LIB.glob("*.so")))

@@ -1,0 +1,498 @@
+/* LolaCUDA kernels: projection packing and volume-tile-stationary
+ * backprojection for sm_103a.
+ *
+ * Method (identical to LolaBunny, HPC-Dwarfs/RabbitCT src/LolaBunny.c:44-75):
+ * for every voxel (i, j, k) at world position O + (i, j, k) * voxelSize and
+ * every projection with matrix a (3x4, column-major):
+ *     w = a2 x + a5 y + a8 z + a11,  u = (a0 x + a3 y + a6 z + a9) / w,
+ *     v = (a1 x + a4 y + a7 z + a10) / w
+ *     vol += 1/w^2 * bilinear(image, u, v)
+ * where bilinear() truncates toward zero ((int)u, so the weight is negative
+ * for u in (-2, 0)) and reads 0 outside the detector (src/LolaBunny.c:11-30).
+ *
+ * GB300 mapping:
+ *  - A CTA owns a tile of 32 (x) x ROWS (y) x VPT (z) voxels.  Each thread
+ *    keeps its VPT voxels (one x column, consecutive z) in registers for a
+ *    whole pass of up to LOLA_MAX_BATCH projections, so the volume crosses HBM
+ *    once per pass instead of once per projection.
+ *  - Per (tile, projection) the tile origin is projected in FP64 (the only
+ *    FP64 work: 11 DFMA).  The homogeneous coordinates are re-centred on an
+ *    FP32 pixel offset c, u' = u - c w, so the FP32 values stepped per voxel
+ *    are small and ix = c + u'/w keeps the precision of ix itself.
+ *  - The 8 tile corners give the tile's detector footprint (the projection of
+ *    a box with w > 0 lies in the convex hull of its corners).  A tile whose
+ *    footprint misses the detector is skipped for that projection (LolaBunny
+ *    adds exact zeros there); one inside the zero margin runs without clamps;
+ *    any other runs the clamped path, which is exact for every voxel.
+ *  - Projections are stored zero-padded by LOLA_MARGIN pixels and stay L2
+ *    resident; taps are gathered through the read-only L1 path.  The quad
+ *    layouts store each pixel's 2x2 neighbourhood together, so one 16 B (FP32)
+ *    or 8 B (FP16/BF16) load fetches all four taps.
+ *  - Floor/index arithmetic avoids the conversion pipe: the stored index is
+ *    formed in FP32 (exact below 2^24) and read from the float's mantissa
+ *    after adding 2^23.
+ */
+#pragma once
+
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "lolacuda_internal.h"
+
+namespace lola {
+
+enum { MODE_SKIP = 0, MODE_FAST = 1, MODE_SLOW = 2 };
+
+/* Per (tile, projection) setup kept in shared memory for the whole pass. */
+struct TileProj {
+  float u0, v0, w0;   /* re-centred homogeneous coordinates at the tile origin */
+  float cu, cv;       /* pixel offsets: ix = cu + u'/w, iy = cv + v'/w */
+  float su[3], sv[3], sw[3]; /* per-axis steps (x, y, z) of u', v', w */
+  int mode;
+  int slot;
+};
+
+__device__ __forceinline__ float rcpApprox(float x)
+{
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+
+__device__ __forceinline__ float bf16LoToFloat(uint32_t x) { return __uint_as_float(x << 16); }
+__device__ __forceinline__ float bf16HiToFloat(uint32_t x) { return __uint_as_float(x & 0xffff0000u); }
+
+/* ---- tap fetch per storage layout ------------------------------------------ */
+
+template <int S> struct Layout;
+
+template <> struct Layout<LOLA_STORE_F32> {
+  typedef float Elem;
+  static constexpr bool kQuad = false;
+  __device__ static __forceinline__ void fetch(const void *img, uint32_t idx, int pitch,
+      float &p00, float &p10, float &p01, float &p11)
+  {
+    const float *f = static_cast<const float *>(img) + idx;
+    p00 = __ldg(f);
+    p10 = __ldg(f + 1);
+    p01 = __ldg(f + pitch);
+    p11 = __ldg(f + pitch + 1);
+  }
+  __device__ static __forceinline__ void store(void *dst, size_t o, float a, float, float, float)
+  {
+    static_cast<float *>(dst)[o] = a;
+  }
+};
+
+template <> struct Layout<LOLA_STORE_F16> {
+  typedef __half Elem;
+  static constexpr bool kQuad = false;
+  __device__ static __forceinline__ void fetch(const void *img, uint32_t idx, int pitch,
+      float &p00, float &p10, float &p01, float &p11)
+  {
+    const __half *h = static_cast<const __half *>(img) + idx;
+    p00 = __half2float(__ldg(h));
+    p10 = __half2float(__ldg(h + 1));
+    p01 = __half2float(__ldg(h + pitch));
+    p11 = __half2float(__ldg(h + pitch + 1));
+  }
+  __device__ static __forceinline__ void store(void *dst, size_t o, float a, float, float, float)
+  {
+    static_cast<__half *>(dst)[o] = __float2half_rn(a);
+  }
+};
+
+template <> struct Layout<LOLA_STORE_BF16> {
+  typedef __nv_bfloat16 Elem;
+  static constexpr bool kQuad = false;
+  __device__ static __forceinline__ void fetch(const void *img, uint32_t idx, int pitch,
+      float &p00, float &p10, float &p01, float &p11)
+  {
+    const unsigned short *h = static_cast<const unsigned short *>(img) + idx;
+    p00 = __uint_as_float((uint32_t)__ldg(h) << 16);
+    p10 = __uint_as_float((uint32_t)__ldg(h + 1) << 16);
+    p01 = __uint_as_float((uint32_t)__ldg(h + pitch) << 16);
+    p11 = __uint_as_float((uint32_t)__ldg(h + pitch + 1) << 16);
+  }
+  __device__ static __forceinline__ void store(void *dst, size_t o, float a, float, float, float)
+  {
+    static_cast<__nv_bfloat16 *>(dst)[o] = __float2bfloat16_rn(a);
+  }
+};
+
+template <> struct Layout<LOLA_STORE_F32Q> {
+  typedef float4 Elem;
+  static constexpr bool kQuad = true;
+  __device__ static __forceinline__ void fetch(const void *img, uint32_t idx, int,
+      float &p00, float &p10, float &p01, float &p11)
+  {
+    const float4 q = __ldg(static_cast<const float4 *>(img) + idx);
+    p00 = q.x;
+    p10 = q.y;
+    p01 = q.z;
+    p11 = q.w;
+  }
+  __device__ static __forceinline__ void store(void *dst, size_t o, float a, float b, float c,
+      float d)
+  {
+    static_cast<float4 *>(dst)[o] = make_float4(a, b, c, d);
+  }
+};
+
+template <> struct Layout<LOLA_STORE_F16Q> {
+  typedef uint2 Elem;
+  static constexpr bool kQuad = true;
+  __device__ static __forceinline__ void fetch(const void *img, uint32_t idx, int,
+      float &p00, float &p10, float &p01, float &p11)
+  {
+    const uint2 q = __ldg(static_cast<const uint2 *>(img) + idx);
+    __half2 lo, hi;
+    lo = *reinterpret_cast<const __half2 *>(&q.x);
+    hi = *reinterpret_cast<const __half2 *>(&q.y);
+    const float2 a = __half22float2(lo);
+    const float2 b = __half22float2(hi);
+    p00 = a.x;
+    p10 = a.y;
+    p01 = b.x;
+    p11 = b.y;
+  }
+  __device__ static __forceinline__ void store(void *dst, size_t o, float a, float b, float c,
+      float d)
+  {
+    const __half2 lo = __floats2half2_rn(a, b);
+    const __half2 hi = __floats2half2_rn(c, d);
+    uint2 q;
+    q.x = *reinterpret_cast<const uint32_t *>(&lo);
+    q.y = *reinterpret_cast<const uint32_t *>(&hi);
+    static_cast<uint2 *>(dst)[o] = q;
+  }
+};
+
+template <> struct Layout<LOLA_STORE_BF16Q> {
+  typedef uint2 Elem;
+  static constexpr bool kQuad = true;
+  __device__ static __forceinline__ void fetch(const void *img, uint32_t idx, int,
+      float &p00, float &p10, float &p01, float &p11)
+  {
+    const uint2 q = __ldg(static_cast<const uint2 *>(img) + idx);
+    p00 = bf16LoToFloat(q.x);
+    p10 = bf16HiToFloat(q.x);
+    p01 = bf16LoToFloat(q.y);
+    p11 = bf16HiToFloat(q.y);
+  }
+  __device__ static __forceinline__ void store(void *dst, size_t o, float a, float b, float c,
+      float d)
+  {
+    const __nv_bfloat162 lo = __floats2bfloat162_rn(a, b);
+    const __nv_bfloat162 hi = __floats2bfloat162_rn(c, d);
+    uint2 q;
+    q.x = *reinterpret_cast<const uint32_t *>(&lo);
+    q.y = *reinterpret_cast<const uint32_t *>(&hi);
+    static_cast<uint2 *>(dst)[o] = q;
+  }
+};
+
+/* ---- packing: FP32 detector image -> zero-padded stored layout ------------- */
+
+struct PackArgs {
+  const float *src;
+  size_t srcStride;   /* floats between consecutive source images */
+  void *ring;
+  size_t slotElems;
+  int slot0;
+  int width, height, margin, pitch, rows;
+};
+
+template <int S>
+__global__ void __launch_bounds__(256) packKernel(const PackArgs a)
+{
+  const int pu = blockIdx.x * 32 + threadIdx.x;
+  const int pv = blockIdx.y * 8 + threadIdx.y;
+  const int p = blockIdx.z;
+  if (pu >= a.pitch || pv >= a.rows)
+    return;
+  const float *img = a.src + (size_t)p * a.srcStride;
+  const int u = pu - a.margin, v = pv - a.margin;
+  auto px = [&](int uu, int vv) -> float {
+    return (uu >= 0 && uu < a.width && vv >= 0 && vv < a.height)
+               ? __ldg(img + (size_t)vv * a.width + uu)
+               : 0.0f;
+  };
+  const size_t o = (size_t)(a.slot0 + p) * a.slotElems + (size_t)pv * a.pitch + pu;
+  if (Layout<S>::kQuad)
+    Layout<S>::store(a.ring, o, px(u, v), px(u + 1, v), px(u, v + 1), px(u + 1, v + 1));
+  else
+    Layout<S>::store(a.ring, o, px(u, v), 0.f, 0.f, 0.f);
+}
+
+/* ---- backprojection pass ---------------------------------------------------- */
+
+struct PassArgs {
+  const void *ring;
+  size_t slotBytes;
+  float *volume;
+  unsigned long long *tileCounters;  /* [skip, fast, slow] or null */
+  int width, height, margin, pitch, rows;
+};
+
+/* Applies one projection to the thread's VPT voxels. */
+template <int S, int VPT, bool KAHAN, bool CLAMP>
+__device__ __forceinline__ void applyProjection(const TileProj &tp, const void *img,
+    const PassArgs &a, float fi, float fj, float (&acc)[VPT], float (&comp)[VPT])
+{
+  const float pitchF = (float)a.pitch;
+  /* index = (ty + M) * pitch + (tx + M), formed as 2^23 + index in FP32 */
+  const float biasF = 8388608.0f + (float)(a.margin * a.pitch + a.margin);
+  const uint32_t maxIdx = Layout<S>::kQuad ? (uint32_t)(a.pitch * a.rows - 1)
+                                           : (uint32_t)(a.pitch * a.rows - a.pitch - 2);
+  const float wLim = (float)(a.width + 1);
+  const float hLim = (float)(a.height + 1);
+
+  const float ut = fmaf(fj, tp.su[1], fmaf(fi, tp.su[0], tp.u0));
+  const float vt = fmaf(fj, tp.sv[1], fmaf(fi, tp.sv[0], tp.v0));
+  const float wt = fmaf(fj, tp.sw[1], fmaf(fi, tp.sw[0], tp.w0));
+#pragma unroll
+  for (int k = 0; k < VPT; ++k) {
+    const float kf = (float)k;
+    const float w = fmaf(kf, tp.sw[2], wt);
+    const float u = fmaf(kf, tp.su[2], ut);
+    const float v = fmaf(kf, tp.sv[2], vt);
+    const float r = rcpApprox(w);
+    float ix = fmaf(u, r, tp.cu);
+    float iy = fmaf(v, r, tp.cv);
+    if (CLAMP) {
+      /* outside [-2, W+1] every tap is in the zero margin, as in LolaBunny */
+      ix = fminf(fmaxf(ix, -2.0f), wLim);
+      iy = fminf(fmaxf(iy, -2.0f), hLim);
+    }
+    const float tx = truncf(ix);  /* (int)x of src/LolaBunny.c:21 */
+    const float ty = truncf(iy);
+    const float ax = ix - tx;
+    const float ay = iy - ty;
+    uint32_t idx = __float_as_uint(fmaf(ty, pitchF, tx + biasF)) - 0x4B000000u;
+    idx = min(idx, maxIdx);  /* memory-safety net; never active on valid input */
+    float p00, p10, p01, p11;
+    Layout<S>::fetch(img, idx, a.pitch, p00, p10, p01, p11);
+    const float b = fmaf(ax, p10 - p00, p00);
+    const float t = fmaf(ax, p11 - p01, p01);
+    const float val = fmaf(ay, t - b, b);
+    float term = val * (r * r);
+    if (CLAMP)
+      term = (val == 0.0f) ? 0.0f : term;  /* w = 0 would give 0 * inf */
+    if (KAHAN) {
+      const float y = term - comp[k];
+      const float s = acc[k] + y;
+      comp[k] = (s - acc[k]) - y;
+      acc[k] = s;
+    } else {
+      acc[k] += term;
+    }
+  }
+}
+
+template <int S, int VPT, int ROWS, bool KAHAN>
+__global__ void __launch_bounds__(32 * ROWS) passKernel(const PassArgs a, const LolaPassParams P)
+{
+  __shared__ TileProj sp[LOLA_MAX_BATCH];
+  const int N = P.N;
+  const int x0 = blockIdx.x * 32, y0 = blockIdx.y * ROWS, z0 = blockIdx.z * VPT;
+  const int tid = threadIdx.y * 32 + threadIdx.x;
+  const int count = P.count;
+
+  /* -- setup A: FP64 projection of the tile origin, one thread per view -- */
+  if (tid < count) {
+    const LolaPassProj &pp = P.proj[tid];
+    const double *m = pp.a;
+    const double vs = (double)P.voxelSize, o = (double)P.originIndex;
+    const double X = o + (double)x0 * vs, Y = o + (double)y0 * vs, Z = o + (double)z0 * vs;
+    const double U = m[0] * X + m[3] * Y + m[6] * Z + m[9];
+    const double V = m[1] * X + m[4] * Y + m[7] * Z + m[10];
+    const double Wd = m[2] * X + m[5] * Y + m[8] * Z + m[11];
+    const float cu = (float)U / (float)Wd;
+    const float cv = (float)V / (float)Wd;
+    TileProj tp;
+    tp.cu = isfinite(cu) ? cu : 0.0f;
+    tp.cv = isfinite(cv) ? cv : 0.0f;
+    tp.u0 = (float)(U - (double)tp.cu * Wd);
+    tp.v0 = (float)(V - (double)tp.cv * Wd);
+    tp.w0 = (float)Wd;
+#pragma unroll
+    for (int ax = 0; ax < 3; ++ax) {
+      tp.sw[ax] = pp.step[ax][2];
+      tp.su[ax] = fmaf(-tp.cu, pp.step[ax][2], pp.step[ax][0]);
+      tp.sv[ax] = fmaf(-tp.cv, pp.step[ax][2], pp.step[ax][1]);
+    }
+    tp.mode = MODE_SLOW;
+    tp.slot = pp.slot;
+    sp[tid] = tp;
+  }
+  __syncthreads();
+
+  /* -- setup B: footprint of the tile from its 8 corners, 8 lanes per view -- */
+  const int ex = min(32, N - x0) - 1, ey = min(ROWS, N - y0) - 1, ez = min(VPT, N - z0) - 1;
+  for (int base = 0; base < 8 * count; base += 32 * ROWS) {
+    const int t = base + tid;
+    const bool active = t < 8 * count;
+    const int p = active ? (t >> 3) : 0;
+    const int c = t & 7;
+    const TileProj &tp = sp[p];
+    const float ox = (c & 1) ? (float)ex : 0.0f;
+    const float oy = (c & 2) ? (float)ey : 0.0f;
+    const float oz = (c & 4) ? (float)ez : 0.0f;
+    const float u = tp.u0 + ox * tp.su[0] + oy * tp.su[1] + oz * tp.su[2];
+    const float v = tp.v0 + ox * tp.sv[0] + oy * tp.sv[1] + oz * tp.sv[2];
+    const float w = tp.w0 + ox * tp.sw[0] + oy * tp.sw[1] + oz * tp.sw[2];
+    const float ix = tp.cu + u / w, iy = tp.cv + v / w;
+    int ok = (w > 0.0f) && isfinite(ix) && isfinite(iy);
+    float mnx = ix, mxx = ix, mny = iy, mxy = iy;
+#pragma unroll
+    for (int s = 1; s < 8; s <<= 1) {
+      mnx = fminf(mnx, __shfl_xor_sync(0xffffffffu, mnx, s));
+      mxx = fmaxf(mxx, __shfl_xor_sync(0xffffffffu, mxx, s));
+      mny = fminf(mny, __shfl_xor_sync(0xffffffffu, mny, s));
+      mxy = fmaxf(mxy, __shfl_xor_sync(0xffffffffu, mxy, s));
+      ok &= __shfl_xor_sync(0xffffffffu, ok, s);
+    }
+    if (active && c == 0) {
+      const float slack = 0.5f;
+      const float W = (float)a.width, H = (float)a.height, M = (float)a.margin;
+      int mode;
+      if (!ok)
+        mode = MODE_SLOW;
+      else if (mxx + slack <= -2.0f || mnx - slack >= W || mxy + slack <= -2.0f ||
+               mny - slack >= H)
+        mode = MODE_SKIP;
+      else if (mnx - slack >= 1.0f - M && mxx + slack <= W + M - 3.0f &&
+               mny - slack >= 1.0f - M && mxy + slack <= H + M - 3.0f)
+        mode = MODE_FAST;
+      else
+        mode = MODE_SLOW;
+      sp[p].mode = mode;
+    }
+  }
+  __syncthreads();
+
+  if (a.tileCounters != nullptr && tid == 0) {
+    unsigned long long nSkip = 0, nFast = 0, nSlow = 0;
+    for (int p = 0; p < count; ++p) {
+      const int m = sp[p].mode;
+      nSkip += (m == MODE_SKIP);
+      nFast += (m == MODE_FAST);
+      nSlow += (m == MODE_SLOW);
+    }
+    atomicAdd(a.tileCounters + 0, nSkip);
+    atomicAdd(a.tileCounters + 1, nFast);
+    atomicAdd(a.tileCounters + 2, nSlow);
+  }
+
+  /* -- main: voxels in registers across the pass -- */
+  const int x = x0 + threadIdx.x, y = y0 + threadIdx.y;
+  const bool inXY = (x < N) && (y < N);
+  const size_t slice = (size_t)N * (size_t)N;
+  float *vcol = a.volume + ((size_t)z0 * N + (size_t)(inXY ? y : 0)) * (size_t)N + (inXY ? x : 0);
+  float acc[VPT], comp[VPT];
+#pragma unroll
+  for (int k = 0; k < VPT; ++k) {
+    acc[k] = (inXY && z0 + k < N) ? vcol[k * slice] : 0.0f;
+    comp[k] = 0.0f;
+  }
+  const float fi = (float)threadIdx.x, fj = (float)threadIdx.y;
+  for (int p = 0; p < count; ++p) {
+    const int mode = sp[p].mode;
+    if (mode == MODE_SKIP)
+      continue;
+    const TileProj tp = sp[p];
+    const void *img = static_cast<const char *>(a.ring) + (size_t)tp.slot * a.slotBytes;
+    if (mode == MODE_FAST)
+      applyProjection<S, VPT, KAHAN, false>(tp, img, a, fi, fj, acc, comp);
+    else
+      applyProjection<S, VPT, KAHAN, true>(tp, img, a, fi, fj, acc, comp);
+  }
+#pragma unroll
+  for (int k = 0; k < VPT; ++k) {
+    if (inXY && z0 + k < N)
+      vcol[k * slice] = KAHAN ? (acc[k] - comp[k]) : acc[k];
+  }
+}
+
+/* ---- host-side launch helpers (instantiated per storage layout) ------------- */
+
+template <int S>
+int launchPack(const LolaStoreDesc *st, const float *src, size_t srcStride, void *ring, int slot0,
+    int count, cudaStream_t stream)
+{
+  PackArgs a;
+  a.src = src;
+  a.srcStride = srcStride;
+  a.ring = ring;
+  a.slotElems = st->slotElems;
+  a.slot0 = slot0;
+  a.width = st->width;
+  a.height = st->height;
+  a.margin = st->margin;
+  a.pitch = st->pitch;
+  a.rows = st->rows;
+  const dim3 block(32, 8);
+  const dim3 grid((st->pitch + 31) / 32, (st->rows + 7) / 8, count);
+  packKernel<S><<<grid, block, 0, stream>>>(a);
+  return (int)cudaGetLastError();
+}
+
+template <int S, int VPT, int ROWS, bool KAHAN>
+int launchPassShape(const PassArgs &a, const LolaPassParams *P, cudaStream_t stream)
+{
+  const int N = P->N;
+  const dim3 block(32, ROWS);
+  const dim3 grid((N + 31) / 32, (N + ROWS - 1) / ROWS, (N + VPT - 1) / VPT);
+  passKernel<S, VPT, ROWS, KAHAN><<<grid, block, 0, stream>>>(a, *P);
+  return (int)cudaGetLastError();
+}
+
+template <int S, bool KAHAN>
+int launchPassAccum(const PassArgs &a, const LolaPassParams *P, cudaStream_t stream)
+{
+  const int vpt = P->voxelsPerThread, rows = P->rowsPerBlock;
+  if (vpt == 8 && rows == 8) return launchPassShape<S, 8, 8, KAHAN>(a, P, stream);
+  if (vpt == 8 && rows == 4) return launchPassShape<S, 8, 4, KAHAN>(a, P, stream);
+  if (vpt == 16 && rows == 8) return launchPassShape<S, 16, 8, KAHAN>(a, P, stream);
+  if (vpt == 16 && rows == 4) return launchPassShape<S, 16, 4, KAHAN>(a, P, stream);
+  if (vpt == 4 && rows == 8) return launchPassShape<S, 4, 8, KAHAN>(a, P, stream);
+  return (int)cudaErrorInvalidConfiguration;
+}
+
+template <int S>
+int launchPass(const LolaStoreDesc *st, const LolaPassParams *P, const void *ring, float *volume,
+    unsigned long long *counters, cudaStream_t stream)
+{
+  PassArgs a;
+  a.ring = ring;
+  a.slotBytes = st->slotElems * (size_t)st->elemBytes;
+  a.volume = volume;
+  a.tileCounters = counters;
+  a.width = st->width;
+  a.height = st->height;
+  a.margin = st->margin;
+  a.pitch = st->pitch;
+  a.rows = st->rows;
+  if (P->accumulation == LOLA_ACCUM_KAHAN)
+    return launchPassAccum<S, true>(a, P, stream);
+  return launchPassAccum<S, false>(a, P, stream);
+}
+
+} /* namespace lola */
+
+#define LOLA_INSTANTIATE_STORAGE(S, NAME)                                                  \
+  extern "C" int lolaLaunchPack_##NAME(const LolaStoreDesc *st, const float *src,          \
+      size_t srcStride, void *ring, int slot0, int count, void *stream)                    \
+  {                                                                                        \
+    return lola::launchPack<S>(st, src, srcStride, ring, slot0, count,                     \
+        static_cast<cudaStream_t>(stream));                                                \
+  }                                                                                        \
+  extern "C" int lolaLaunchPass_##NAME(const LolaStoreDesc *st, const LolaPassParams *P,   \
+      const void *ring, float *volume, unsigned long long *counters, void *stream)         \
+  {                                                                                        \
+    return lola::launchPass<S>(st, P, ring, volume, counters,                              \
+        static_cast<cudaStream_t>(stream));                                                \
+  }

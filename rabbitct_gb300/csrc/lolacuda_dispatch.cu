@@ -1,0 +1,60 @@
+/* Dispatch from the C host code to the per-layout kernel launchers. */
+#include <cuda_runtime.h>
+
+#include "lolacuda_internal.h"
+
+#define LOLA_DECLARE(NAME)                                                                 \
+  extern "C" int lolaLaunchPack_##NAME(const LolaStoreDesc *, const float *, size_t,       \
+      void *, int, int, void *);                                                           \
+  extern "C" int lolaLaunchPass_##NAME(const LolaStoreDesc *, const LolaPassParams *,      \
+      const void *, float *, unsigned long long *, void *);
+
+LOLA_DECLARE(F32)
+LOLA_DECLARE(F16)
+LOLA_DECLARE(BF16)
+LOLA_DECLARE(F32Q)
+LOLA_DECLARE(F16Q)
+LOLA_DECLARE(BF16Q)
+
+static_assert(sizeof(LolaPassParams) < 32000, "pass parameters exceed the kernel parameter limit");
+
+extern "C" int lolaLaunchPack(const LolaStoreDesc *st, const float *d_src, size_t srcStride,
+    void *d_ring, int slot0, int count, void *stream)
+{
+  if (count <= 0)
+    return 0;
+  switch (st->storage) {
+  case LOLA_STORE_F32: return lolaLaunchPack_F32(st, d_src, srcStride, d_ring, slot0, count, stream);
+  case LOLA_STORE_F16: return lolaLaunchPack_F16(st, d_src, srcStride, d_ring, slot0, count, stream);
+  case LOLA_STORE_BF16: return lolaLaunchPack_BF16(st, d_src, srcStride, d_ring, slot0, count, stream);
+  case LOLA_STORE_F32Q: return lolaLaunchPack_F32Q(st, d_src, srcStride, d_ring, slot0, count, stream);
+  case LOLA_STORE_F16Q: return lolaLaunchPack_F16Q(st, d_src, srcStride, d_ring, slot0, count, stream);
+  case LOLA_STORE_BF16Q: return lolaLaunchPack_BF16Q(st, d_src, srcStride, d_ring, slot0, count, stream);
+  default: return (int)cudaErrorInvalidValue;
+  }
+}
+
+extern "C" int lolaLaunchBackproject(const LolaStoreDesc *st, const LolaPassParams *P,
+    const void *d_ring, float *d_volume, unsigned long long *d_tileCounters, void *stream)
+{
+  if (P->count <= 0)
+    return 0;
+  if (P->count > LOLA_MAX_BATCH)
+    return (int)cudaErrorInvalidValue;
+  switch (st->storage) {
+  case LOLA_STORE_F32: return lolaLaunchPass_F32(st, P, d_ring, d_volume, d_tileCounters, stream);
+  case LOLA_STORE_F16: return lolaLaunchPass_F16(st, P, d_ring, d_volume, d_tileCounters, stream);
+  case LOLA_STORE_BF16: return lolaLaunchPass_BF16(st, P, d_ring, d_volume, d_tileCounters, stream);
+  case LOLA_STORE_F32Q: return lolaLaunchPass_F32Q(st, P, d_ring, d_volume, d_tileCounters, stream);
+  case LOLA_STORE_F16Q: return lolaLaunchPass_F16Q(st, P, d_ring, d_volume, d_tileCounters, stream);
+  case LOLA_STORE_BF16Q: return lolaLaunchPass_BF16Q(st, P, d_ring, d_volume, d_tileCounters, stream);
+  default: return (int)cudaErrorInvalidValue;
+  }
+}
+
+extern "C" int lolaKernelShapeSupported(int voxelsPerThread, int rowsPerBlock)
+{
+  return (voxelsPerThread == 8 && (rowsPerBlock == 8 || rowsPerBlock == 4)) ||
+         (voxelsPerThread == 16 && (rowsPerBlock == 8 || rowsPerBlock == 4)) ||
+         (voxelsPerThread == 4 && rowsPerBlock == 8);
+}

@@ -1,0 +1,682 @@
+/* LolaCUDA host code (C99): the RabbitCT module API, configuration and the
+ * plan API declared in include/lolaCuda.h.
+ *
+ * Data layout in device memory (one plan):
+ *   volume   N^3 FP32, x fastest, identical to the runner's volumeData so the
+ *            final copy is one contiguous transfer (src/rabbitRunner.c:192)
+ *   ring     `batch` stored projections, each zero-padded by LOLA_MARGIN
+ *            pixels in the configured storage layout
+ *   stage    `batch` raw FP32 detector images, landing zone of host uploads
+ *   counters 3 x u64 (tile statistics)
+ *
+ * Module state follows the reference modules: one static instance per
+ * process (the reference modules keep their padding and line ranges in file
+ * statics too, e.g. src/LolaOPT.c:18-21).
+ */
+#define _POSIX_C_SOURCE 200809L
+#include <ctype.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <cuda_runtime_api.h>
+
+#include "lolaCuda.h"
+#include "lolacuda_internal.h"
+
+/* ---- errors ---------------------------------------------------------------- */
+
+static __thread char gLastError[512];
+
+static int setError(const char *fmt, ...)
+{
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(gLastError, sizeof(gLastError), fmt, ap);
+  va_end(ap);
+  return 0;
+}
+
+const char *lolaCudaLastError(void)
+{
+  return gLastError;
+}
+
+#define CUDA_TRY(call)                                                                   \
+  do {                                                                                   \
+    cudaError_t e_ = (call);                                                             \
+    if (e_ != cudaSuccess)                                                               \
+      return setError("%s:%d: %s: %s", __FILE__, __LINE__, #call, cudaGetErrorString(e_)); \
+  } while (0)
+
+#define LAUNCH_TRY(call)                                                                 \
+  do {                                                                                   \
+    int e_ = (call);                                                                     \
+    if (e_ != 0)                                                                         \
+      return setError("%s:%d: kernel launch failed: %s", __FILE__, __LINE__,             \
+          cudaGetErrorString((cudaError_t)e_));                                          \
+  } while (0)
+
+/* ---- configuration ---------------------------------------------------------- */
+
+static int storageFromName(const char *s)
+{
+  static const char *names[] = { "f32", "f16", "bf16", "f32q", "f16q", "bf16q" };
+  for (int i = 0; i < 6; i++) {
+    const char *a = names[i], *b = s;
+    while (*a && *b && tolower((unsigned char)*b) == *a) {
+      a++;
+      b++;
+    }
+    if (*a == 0 && *b == 0)
+      return i;
+  }
+  return -1;
+}
+
+static int envInt(const char *name, int dflt)
+{
+  const char *v = getenv(name);
+  if (v == NULL || *v == 0)
+    return dflt;
+  return atoi(v);
+}
+
+void lolaCudaDefaultConfig(LolaCudaConfig *c)
+{
+  memset(c, 0, sizeof(*c));
+  c->storage = LOLA_STORE_F32;
+  c->accumulation = LOLA_ACCUM_PLAIN;
+  c->batch = 16;
+  c->voxelsPerThread = 8;
+  c->rowsPerBlock = 8;
+  c->syncEachCall = 1;
+  c->exitOnError = 1;
+  c->collectStats = 0;
+  c->device = 0;
+  const char *s = getenv("LOLACUDA_STORAGE");
+  if (s != NULL && storageFromName(s) >= 0)
+    c->storage = storageFromName(s);
+  const char *acc = getenv("LOLACUDA_ACCUM");
+  if (acc != NULL && strcmp(acc, "kahan") == 0)
+    c->accumulation = LOLA_ACCUM_KAHAN;
+  c->batch = envInt("LOLACUDA_BATCH", c->batch);
+  c->voxelsPerThread = envInt("LOLACUDA_VPT", c->voxelsPerThread);
+  c->rowsPerBlock = envInt("LOLACUDA_ROWS", c->rowsPerBlock);
+  c->syncEachCall = envInt("LOLACUDA_SYNC", c->syncEachCall);
+  c->exitOnError = envInt("LOLACUDA_EXIT", c->exitOnError);
+}
+
+static int validateConfig(const LolaCudaConfig *c)
+{
+  if (c->storage < LOLA_STORE_F32 || c->storage > LOLA_STORE_BF16Q)
+    return setError("invalid storage %d", c->storage);
+  if (c->accumulation != LOLA_ACCUM_PLAIN && c->accumulation != LOLA_ACCUM_KAHAN)
+    return setError("invalid accumulation %d", c->accumulation);
+  if (c->batch < 1 || c->batch > LOLA_MAX_BATCH)
+    return setError("batch %d outside 1..%d", c->batch, LOLA_MAX_BATCH);
+  if (!lolaKernelShapeSupported(c->voxelsPerThread, c->rowsPerBlock))
+    return setError("no kernel for %d voxels per thread x %d rows per block",
+        c->voxelsPerThread, c->rowsPerBlock);
+  return 1;
+}
+
+static LolaCudaConfig gConfig;
+static int gConfigSet = 0;
+
+int lolaCudaSetConfig(const LolaCudaConfig *c)
+{
+  if (c == NULL)
+    return setError("null config");
+  if (!validateConfig(c))
+    return 0;
+  gConfig = *c;
+  gConfigSet = 1;
+  return 1;
+}
+
+int lolaCudaGetConfig(LolaCudaConfig *c)
+{
+  if (!gConfigSet) {
+    lolaCudaDefaultConfig(&gConfig);
+    gConfigSet = 1;
+  }
+  *c = gConfig;
+  return 1;
+}
+
+/* ---- plan --------------------------------------------------------------------- */
+
+typedef struct {
+  cudaEvent_t start, stop;
+} EventPair;
+
+struct LolaCudaPlan {
+  LolaCudaGeometry geom;
+  LolaCudaConfig cfg;
+  LolaStoreDesc store;
+  int device;
+  cudaStream_t stream;      /* packing + passes */
+  cudaStream_t copyStream;  /* host uploads into the stage */
+  cudaEvent_t stageFree;    /* stage consumed by the last pack */
+  cudaEvent_t stageReady;   /* uploads of the pending batch done */
+  float *d_volume;
+  void *d_ring;
+  float *d_stage;
+  unsigned long long *d_counters;
+  size_t imageElems;
+  /* host-staged batch (module API / BackprojectHost) */
+  int pending;
+  double pendingMats[LOLA_MAX_BATCH][12];
+  /* statistics */
+  LolaCudaStats stats;
+  EventPair *events;
+  int nEvents, capEvents;
+};
+
+static int elemBytesOf(int storage)
+{
+  switch (storage) {
+  case LOLA_STORE_F32: return 4;
+  case LOLA_STORE_F16: return 2;
+  case LOLA_STORE_BF16: return 2;
+  case LOLA_STORE_F32Q: return 16;
+  case LOLA_STORE_F16Q: return 8;
+  case LOLA_STORE_BF16Q: return 8;
+  default: return 0;
+  }
+}
+
+static int planRelease(LolaCudaPlan *p)
+{
+  if (p == NULL)
+    return 1;
+  cudaSetDevice(p->device);
+  if (p->stream)
+    cudaStreamSynchronize(p->stream);
+  if (p->copyStream)
+    cudaStreamSynchronize(p->copyStream);
+  for (int i = 0; i < p->nEvents; i++) {
+    cudaEventDestroy(p->events[i].start);
+    cudaEventDestroy(p->events[i].stop);
+  }
+  free(p->events);
+  cudaFree(p->d_volume);
+  cudaFree(p->d_ring);
+  cudaFree(p->d_stage);
+  cudaFree(p->d_counters);
+  if (p->stageFree)
+    cudaEventDestroy(p->stageFree);
+  if (p->stageReady)
+    cudaEventDestroy(p->stageReady);
+  if (p->stream)
+    cudaStreamDestroy(p->stream);
+  if (p->copyStream)
+    cudaStreamDestroy(p->copyStream);
+  free(p);
+  return 1;
+}
+
+int lolaCudaPlanDestroy(LolaCudaPlan *p)
+{
+  return planRelease(p);
+}
+
+static int planInit(LolaCudaPlan *p)
+{
+  const LolaCudaGeometry *g = &p->geom;
+  CUDA_TRY(cudaSetDevice(p->device));
+  CUDA_TRY(cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking));
+  CUDA_TRY(cudaStreamCreateWithFlags(&p->copyStream, cudaStreamNonBlocking));
+  CUDA_TRY(cudaEventCreateWithFlags(&p->stageFree, cudaEventDisableTiming));
+  CUDA_TRY(cudaEventCreateWithFlags(&p->stageReady, cudaEventDisableTiming));
+
+  LolaStoreDesc *s = &p->store;
+  s->storage = p->cfg.storage;
+  s->elemBytes = elemBytesOf(s->storage);
+  s->margin = LOLA_MARGIN;
+  s->width = g->imageWidth;
+  s->height = g->imageHeight;
+  s->pitch = g->imageWidth + 2 * LOLA_MARGIN;
+  s->rows = g->imageHeight + 2 * LOLA_MARGIN;
+  /* index arithmetic in the kernel is exact below 2^23 pixels */
+  if ((long long)s->pitch * s->rows >= (1LL << 23) - 2 * (long long)s->pitch)
+    return setError("detector %dx%d too large (padded image must stay below 2^23 pixels)",
+        g->imageWidth, g->imageHeight);
+  const size_t px = (size_t)s->pitch * (size_t)s->rows;
+  s->slotElems = (px + 63) & ~(size_t)63;
+  p->imageElems = (size_t)g->imageWidth * (size_t)g->imageHeight;
+
+  const size_t nvox = (size_t)g->problemSize * g->problemSize * g->problemSize;
+  CUDA_TRY(cudaMalloc((void **)&p->d_volume, nvox * sizeof(float)));
+  CUDA_TRY(cudaMemsetAsync(p->d_volume, 0, nvox * sizeof(float), p->stream));
+  CUDA_TRY(cudaMalloc(&p->d_ring, (size_t)p->cfg.batch * s->slotElems * s->elemBytes));
+  CUDA_TRY(cudaMemsetAsync(p->d_ring, 0, (size_t)p->cfg.batch * s->slotElems * s->elemBytes,
+      p->stream));
+  CUDA_TRY(cudaMalloc((void **)&p->d_stage, (size_t)p->cfg.batch * p->imageElems * sizeof(float)));
+  CUDA_TRY(cudaMalloc((void **)&p->d_counters, 3 * sizeof(unsigned long long)));
+  CUDA_TRY(cudaMemsetAsync(p->d_counters, 0, 3 * sizeof(unsigned long long), p->stream));
+  CUDA_TRY(cudaEventRecord(p->stageFree, p->stream));
+  CUDA_TRY(cudaStreamSynchronize(p->stream));
+  return 1;
+}
+
+int lolaCudaPlanCreate(const LolaCudaGeometry *g, const LolaCudaConfig *cfg, LolaCudaPlan **out)
+{
+  if (out == NULL || g == NULL)
+    return setError("null argument");
+  *out = NULL;
+  LolaCudaConfig c;
+  if (cfg != NULL)
+    c = *cfg;
+  else
+    lolaCudaDefaultConfig(&c);
+  if (!validateConfig(&c))
+    return 0;
+  if (g->problemSize <= 0 || g->imageWidth <= 0 || g->imageHeight <= 0)
+    return setError("invalid geometry N=%d W=%d H=%d", g->problemSize, g->imageWidth,
+        g->imageHeight);
+  if (g->problemSize > 2048)
+    return setError("problem size %d above the supported 2048", g->problemSize);
+  if (!(g->voxelSize > 0.0f))
+    return setError("voxel size must be positive");
+  LolaCudaPlan *p = (LolaCudaPlan *)calloc(1, sizeof(LolaCudaPlan));
+  if (p == NULL)
+    return setError("out of host memory");
+  p->geom = *g;
+  p->cfg = c;
+  p->device = c.device;
+  if (!planInit(p)) {
+    char msg[512];
+    snprintf(msg, sizeof(msg), "%s", gLastError);
+    planRelease(p);
+    return setError("%s", msg);
+  }
+  *out = p;
+  return 1;
+}
+
+float *lolaCudaPlanVolume(LolaCudaPlan *p)
+{
+  return p ? p->d_volume : NULL;
+}
+
+void *lolaCudaPlanStream(LolaCudaPlan *p)
+{
+  return p ? (void *)p->stream : NULL;
+}
+
+static size_t volumeBytes(const LolaCudaPlan *p)
+{
+  const size_t n = (size_t)p->geom.problemSize;
+  return n * n * n * sizeof(float);
+}
+
+int lolaCudaPlanZeroVolume(LolaCudaPlan *p)
+{
+  if (p == NULL)
+    return setError("null plan");
+  CUDA_TRY(cudaSetDevice(p->device));
+  CUDA_TRY(cudaMemsetAsync(p->d_volume, 0, volumeBytes(p), p->stream));
+  return 1;
+}
+
+int lolaCudaPlanUploadVolume(LolaCudaPlan *p, const float *h)
+{
+  if (p == NULL || h == NULL)
+    return setError("null argument");
+  CUDA_TRY(cudaSetDevice(p->device));
+  CUDA_TRY(cudaMemcpyAsync(p->d_volume, h, volumeBytes(p), cudaMemcpyHostToDevice, p->stream));
+  CUDA_TRY(cudaStreamSynchronize(p->stream));
+  return 1;
+}
+
+int lolaCudaPlanDownloadVolume(LolaCudaPlan *p, float *h)
+{
+  if (p == NULL || h == NULL)
+    return setError("null argument");
+  CUDA_TRY(cudaSetDevice(p->device));
+  CUDA_TRY(cudaMemcpyAsync(h, p->d_volume, volumeBytes(p), cudaMemcpyDeviceToHost, p->stream));
+  CUDA_TRY(cudaStreamSynchronize(p->stream));
+  return 1;
+}
+
+/* FP32 voxel steps of one view: step[axis][comp] = a[axis*3 + comp] * voxelSize */
+static void fillPassProj(LolaPassProj *pp, const double *m, float voxelSize, int slot)
+{
+  memcpy(pp->a, m, 12 * sizeof(double));
+  for (int ax = 0; ax < 3; ax++)
+    for (int c = 0; c < 3; c++)
+      pp->step[ax][c] = (float)(m[ax * 3 + c] * (double)voxelSize);
+  pp->slot = slot;
+}
+
+static int pushEvent(LolaCudaPlan *p, EventPair **out)
+{
+  if (p->nEvents == p->capEvents) {
+    const int cap = p->capEvents ? 2 * p->capEvents : 64;
+    EventPair *e = (EventPair *)realloc(p->events, (size_t)cap * sizeof(EventPair));
+    if (e == NULL)
+      return setError("out of host memory");
+    p->events = e;
+    p->capEvents = cap;
+  }
+  EventPair *e = &p->events[p->nEvents];
+  CUDA_TRY(cudaEventCreate(&e->start));
+  CUDA_TRY(cudaEventCreate(&e->stop));
+  p->nEvents++;
+  *out = e;
+  return 1;
+}
+
+/* One backprojection pass over ring slots [0, count) with the given matrices. */
+static int launchPass(LolaCudaPlan *p, const double *mats, int count)
+{
+  LolaPassParams P;
+  memset(&P, 0, sizeof(P));
+  P.N = p->geom.problemSize;
+  P.count = count;
+  P.voxelSize = p->geom.voxelSize;
+  P.originIndex = p->geom.originIndex;
+  P.accumulation = p->cfg.accumulation;
+  P.voxelsPerThread = p->cfg.voxelsPerThread;
+  P.rowsPerBlock = p->cfg.rowsPerBlock;
+  P.countTiles = p->cfg.collectStats;
+  for (int i = 0; i < count; i++)
+    fillPassProj(&P.proj[i], mats + 12 * (size_t)i, p->geom.voxelSize, i);
+  EventPair *ev = NULL;
+  if (p->cfg.collectStats) {
+    if (!pushEvent(p, &ev))
+      return 0;
+    CUDA_TRY(cudaEventRecord(ev->start, p->stream));
+  }
+  LAUNCH_TRY(lolaLaunchBackproject(&p->store, &P, p->d_ring, p->d_volume,
+      p->cfg.collectStats ? p->d_counters : NULL, p->stream));
+  if (ev != NULL)
+    CUDA_TRY(cudaEventRecord(ev->stop, p->stream));
+  p->stats.passes++;
+  p->stats.projections += count;
+  return 1;
+}
+
+int lolaCudaPlanBackprojectDevice(LolaCudaPlan *p, const float *d_images, size_t imageStride,
+    const double *h_mats, int count)
+{
+  if (p == NULL || d_images == NULL || h_mats == NULL)
+    return setError("null argument");
+  if (count < 0)
+    return setError("negative projection count");
+  if (p->pending != 0)
+    return setError("host-staged projections pending; synchronize the plan first");
+  CUDA_TRY(cudaSetDevice(p->device));
+  for (int done = 0; done < count;) {
+    const int n = (count - done < p->cfg.batch) ? count - done : p->cfg.batch;
+    LAUNCH_TRY(lolaLaunchPack(&p->store, d_images + (size_t)done * imageStride, imageStride,
+        p->d_ring, 0, n, p->stream));
+    p->stats.packs++;
+    if (!launchPass(p, h_mats + 12 * (size_t)done, n))
+      return 0;
+    done += n;
+  }
+  return 1;
+}
+
+/* Packs and backprojects the host-staged batch. */
+static int flushPending(LolaCudaPlan *p)
+{
+  if (p->pending == 0)
+    return 1;
+  CUDA_TRY(cudaEventRecord(p->stageReady, p->copyStream));
+  CUDA_TRY(cudaStreamWaitEvent(p->stream, p->stageReady, 0));
+  LAUNCH_TRY(lolaLaunchPack(&p->store, p->d_stage, p->imageElems, p->d_ring, 0, p->pending,
+      p->stream));
+  p->stats.packs++;
+  CUDA_TRY(cudaEventRecord(p->stageFree, p->stream));
+  const int n = p->pending;
+  p->pending = 0;
+  return launchPass(p, &p->pendingMats[0][0], n);
+}
+
+/* Stages one host projection; flushes when the ring is full. */
+static int stageHost(LolaCudaPlan *p, const float *image, const double *matrix, int *flushed)
+{
+  if (p->pending == 0)
+    CUDA_TRY(cudaStreamWaitEvent(p->copyStream, p->stageFree, 0));
+  CUDA_TRY(cudaMemcpyAsync(p->d_stage + (size_t)p->pending * p->imageElems, image,
+      p->imageElems * sizeof(float), cudaMemcpyHostToDevice, p->copyStream));
+  memcpy(p->pendingMats[p->pending], matrix, 12 * sizeof(double));
+  p->pending++;
+  if (p->pending == p->cfg.batch) {
+    if (!flushPending(p))
+      return 0;
+    *flushed = 1;
+  }
+  return 1;
+}
+
+int lolaCudaPlanBackprojectHost(LolaCudaPlan *p, const float *h_images, size_t imageStride,
+    const double *h_mats, int count)
+{
+  if (p == NULL || h_images == NULL || h_mats == NULL)
+    return setError("null argument");
+  CUDA_TRY(cudaSetDevice(p->device));
+  int flushed = 0;
+  for (int i = 0; i < count; i++)
+    if (!stageHost(p, h_images + (size_t)i * imageStride, h_mats + 12 * (size_t)i, &flushed))
+      return 0;
+  if (!flushPending(p))
+    return 0;
+  CUDA_TRY(cudaStreamSynchronize(p->copyStream));
+  return 1;
+}
+
+static int collectEvents(LolaCudaPlan *p)
+{
+  for (int i = 0; i < p->nEvents; i++) {
+    float ms = 0.0f;
+    CUDA_TRY(cudaEventSynchronize(p->events[i].stop));
+    CUDA_TRY(cudaEventElapsedTime(&ms, p->events[i].start, p->events[i].stop));
+    p->stats.passMs += ms;
+    cudaEventDestroy(p->events[i].start);
+    cudaEventDestroy(p->events[i].stop);
+  }
+  p->nEvents = 0;
+  return 1;
+}
+
+int lolaCudaPlanSynchronize(LolaCudaPlan *p)
+{
+  if (p == NULL)
+    return setError("null plan");
+  CUDA_TRY(cudaSetDevice(p->device));
+  if (!flushPending(p))
+    return 0;
+  CUDA_TRY(cudaStreamSynchronize(p->copyStream));
+  CUDA_TRY(cudaStreamSynchronize(p->stream));
+  return 1;
+}
+
+int lolaCudaPlanGetStats(LolaCudaPlan *p, LolaCudaStats *out)
+{
+  if (p == NULL || out == NULL)
+    return setError("null argument");
+  if (!lolaCudaPlanSynchronize(p))
+    return 0;
+  if (!collectEvents(p))
+    return 0;
+  unsigned long long c[3] = { 0, 0, 0 };
+  CUDA_TRY(cudaMemcpy(c, p->d_counters, sizeof(c), cudaMemcpyDeviceToHost));
+  p->stats.tilePassesSkipped = (int64_t)c[0];
+  p->stats.tilePassesFast = (int64_t)c[1];
+  p->stats.tilePassesSlow = (int64_t)c[2];
+  *out = p->stats;
+  return 1;
+}
+
+int lolaCudaPlanResetStats(LolaCudaPlan *p)
+{
+  if (p == NULL)
+    return setError("null plan");
+  if (!lolaCudaPlanSynchronize(p) || !collectEvents(p))
+    return 0;
+  memset(&p->stats, 0, sizeof(p->stats));
+  CUDA_TRY(cudaMemset(p->d_counters, 0, 3 * sizeof(unsigned long long)));
+  return 1;
+}
+
+/* ---- device helpers ------------------------------------------------------------ */
+
+void *lolaCudaDeviceAlloc(size_t bytes)
+{
+  void *d = NULL;
+  cudaError_t e = cudaMalloc(&d, bytes);
+  if (e != cudaSuccess) {
+    setError("cudaMalloc(%zu): %s", bytes, cudaGetErrorString(e));
+    return NULL;
+  }
+  return d;
+}
+
+int lolaCudaDeviceFree(void *d)
+{
+  CUDA_TRY(cudaFree(d));
+  return 1;
+}
+
+int lolaCudaCopyToDevice(void *d, const void *h, size_t bytes)
+{
+  CUDA_TRY(cudaMemcpy(d, h, bytes, cudaMemcpyHostToDevice));
+  return 1;
+}
+
+int lolaCudaCopyToHost(void *h, const void *d, size_t bytes)
+{
+  CUDA_TRY(cudaMemcpy(h, d, bytes, cudaMemcpyDeviceToHost));
+  return 1;
+}
+
+int lolaCudaDeviceSynchronize(void)
+{
+  CUDA_TRY(cudaDeviceSynchronize());
+  return 1;
+}
+
+/* ---- RabbitCT module API ------------------------------------------------------- */
+
+static LolaCudaPlan *gPlan = NULL;
+static uint32_t gTotalProjections = 0; /* known with -a (src/rabbitRunner.c:209-210) */
+static int gExitOnError = 1;
+
+static int moduleFail(const char *where)
+{
+  fprintf(stderr, "LolaCUDA %s: %s\n", where, gLastError);
+  fflush(stderr);
+  if (gExitOnError)
+    exit(EXIT_FAILURE);
+  return 0;
+}
+
+int lolaCudaPrepare(RabbitCtGlobalData *d)
+{
+  LolaCudaConfig c;
+  lolaCudaGetConfig(&c);
+  gExitOnError = c.exitOnError;
+  if (d == NULL) {
+    setError("null global data");
+    return moduleFail("prepare");
+  }
+  if (gPlan != NULL) {
+    planRelease(gPlan);
+    gPlan = NULL;
+  }
+  LolaCudaGeometry g;
+  g.problemSize = (int32_t)d->problemSize;
+  g.imageWidth = (int32_t)d->imageWidth;
+  g.imageHeight = (int32_t)d->imageHeight;
+  g.voxelSize = d->voxelSize;
+  g.originIndex = d->O_Index;
+  if (d->volumeData == NULL) {
+    setError("volumeData is null");
+    return moduleFail("prepare");
+  }
+  if (!lolaCudaPlanCreate(&g, &c, &gPlan))
+    return moduleFail("prepare");
+  /* the module accumulates into whatever the caller's volume holds, like
+     LolaBunny's `+=` (src/LolaBunny.c:68) */
+  if (!lolaCudaPlanUploadVolume(gPlan, d->volumeData))
+    return moduleFail("prepare");
+  gTotalProjections = d->numberOfProjections;
+  return 1;
+}
+
+int lolaCudaBackprojection(RabbitCtGlobalData *d)
+{
+  if (gPlan == NULL) {
+    setError("backprojection called before prepare");
+    return moduleFail("backprojection");
+  }
+  if (d == NULL || (d->numberOfProjections > 0 && d->projectionBuffer == NULL)) {
+    setError("no projection buffer");
+    return moduleFail("backprojection");
+  }
+  if ((int32_t)d->imageWidth != gPlan->geom.imageWidth ||
+      (int32_t)d->imageHeight != gPlan->geom.imageHeight ||
+      (int32_t)d->problemSize != gPlan->geom.problemSize) {
+    setError("geometry changed between prepare and backprojection");
+    return moduleFail("backprojection");
+  }
+  LolaCudaPlan *p = gPlan;
+  if (cudaSetDevice(p->device) != cudaSuccess) {
+    setError("cudaSetDevice failed");
+    return moduleFail("backprojection");
+  }
+  int flushed = 0;
+  for (uint32_t i = 0; i < d->numberOfProjections; i++) {
+    const Projection *pr = &d->projectionBuffer[i];
+    if (pr->image == NULL || pr->matrix == NULL) {
+      setError("projection %u has no image or matrix", i);
+      return moduleFail("backprojection");
+    }
+    if (!stageHost(p, pr->image, pr->matrix, &flushed))
+      return moduleFail("backprojection");
+    /* the last view of the scan closes the pass, so no work is left for the
+       untimed finish (src/rabbitRunner.c:287) */
+    if (gTotalProjections > 0 && pr->id >= (int)gTotalProjections && p->pending > 0) {
+      if (!flushPending(p))
+        return moduleFail("backprojection");
+      flushed = 1;
+    }
+  }
+  /* the runner reuses its buffers after we return (src/rabbitRunner.c:275-278) */
+  if (cudaStreamSynchronize(p->copyStream) != cudaSuccess) {
+    setError("upload failed: %s", cudaGetErrorString(cudaGetLastError()));
+    return moduleFail("backprojection");
+  }
+  if (flushed && p->cfg.syncEachCall) {
+    cudaError_t e = cudaStreamSynchronize(p->stream);
+    if (e != cudaSuccess) {
+      setError("pass failed: %s", cudaGetErrorString(e));
+      return moduleFail("backprojection");
+    }
+  }
+  return 1;
+}
+
+int lolaCudaFinish(RabbitCtGlobalData *d)
+{
+  if (gPlan == NULL) {
+    setError("finish called before prepare");
+    return moduleFail("finish");
+  }
+  if (d == NULL || d->volumeData == NULL) {
+    setError("volumeData is null");
+    return moduleFail("finish");
+  }
+  if (!lolaCudaPlanSynchronize(gPlan) || !lolaCudaPlanDownloadVolume(gPlan, d->volumeData))
+    return moduleFail("finish");
+  planRelease(gPlan);
+  gPlan = NULL;
+  gTotalProjections = 0;
+  return 1;
+}

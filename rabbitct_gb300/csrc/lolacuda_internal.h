@@ -1,0 +1,69 @@
+/* Internal interface between the C host code (lolacuda_host.c) and the CUDA
+ * kernels (lolacuda_kernels.cu).  Plain C types only. */
+#ifndef LOLACUDA_INTERNAL_H
+#define LOLACUDA_INTERNAL_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#include "lolaCuda.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Zero margin around every stored projection, in pixels.  Taps outside the
+ * detector read these zeros, which is LolaBunny's pN() = 0 outside the image
+ * (src/LolaBunny.c:11-17).  A (tile, projection) pair whose footprint lies
+ * inside the margin runs without coordinate clamps. */
+#define LOLA_MARGIN 64
+
+/* Stored (padded) projection layout on the device. */
+typedef struct {
+  int32_t storage;      /* LOLA_STORE_* */
+  int32_t elemBytes;    /* bytes per stored pixel (quad layouts: 4 taps) */
+  int32_t margin;       /* LOLA_MARGIN */
+  int32_t pitch;        /* padded width, pixels */
+  int32_t rows;         /* padded height, pixels */
+  int32_t width;        /* detector width */
+  int32_t height;       /* detector height */
+  int32_t reserved;
+  size_t slotElems;     /* pixels per ring slot (>= pitch * rows, 256 B multiple) */
+} LolaStoreDesc;
+
+/* One projection of a kernel pass: the FP64 matrix and its FP32 voxel steps. */
+typedef struct {
+  double a[12];         /* column-major 3x4, a[col*3 + row] */
+  float step[3][3];     /* step[axis][comp]: (float)(a[axis*3 + comp] * voxelSize) */
+  int32_t slot;         /* ring slot holding the stored image */
+  int32_t reserved[3];
+} LolaPassProj;
+
+typedef struct {
+  int32_t N;
+  int32_t count;        /* projections in this pass, 1..LOLA_MAX_BATCH */
+  float voxelSize;
+  float originIndex;
+  int32_t accumulation; /* LOLA_ACCUM_* */
+  int32_t voxelsPerThread;
+  int32_t rowsPerBlock;
+  int32_t countTiles;   /* accumulate fast/slow/skipped tile counters */
+  LolaPassProj proj[LOLA_MAX_BATCH];
+} LolaPassParams;
+
+/* Kernel launchers (lolacuda_kernels.cu).  Return 0 on success or a
+ * cudaError_t value. */
+int lolaLaunchPack(const LolaStoreDesc *store, const float *d_src, size_t srcStride,
+    void *d_ring, int slot0, int count, void *stream);
+
+int lolaLaunchBackproject(const LolaStoreDesc *store, const LolaPassParams *params,
+    const void *d_ring, float *d_volume, unsigned long long *d_tileCounters, void *stream);
+
+/* 1 if the (voxelsPerThread, rowsPerBlock) pair has a compiled kernel. */
+int lolaKernelShapeSupported(int voxelsPerThread, int rowsPerBlock);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* LOLACUDA_INTERNAL_H */

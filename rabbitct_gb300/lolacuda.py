@@ -1,0 +1,175 @@
+"""Python front end of LolaCUDA: the plan API and RabbitCtGlobalData helpers.
+
+Everything calls liblolacuda.so through its C ABI (include/lolaCuda.h); there
+is no Python or CPU implementation of the backprojection in this package.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _native
+from ._native import (LolaCudaConfig, LolaCudaGeometry, LolaCudaStats, Projection,
+                      RabbitCtGlobalData, check, config, load_lolacuda)
+
+__all__ = ["Plan", "DeviceBuffer", "GlobalData", "module_functions", "config"]
+
+
+class DeviceBuffer:
+    """A cudaMalloc'ed buffer owned by Python (via lolaCudaDeviceAlloc)."""
+
+    def __init__(self, nbytes: int):
+        self.lib = load_lolacuda()
+        self.nbytes = int(nbytes)
+        self.ptr = self.lib.lolaCudaDeviceAlloc(self.nbytes)
+        if not self.ptr:
+            raise _native.LolaCudaError(f"device alloc: {_native.last_error()}")
+
+    @classmethod
+    def from_array(cls, a: np.ndarray) -> "DeviceBuffer":
+        a = np.ascontiguousarray(a)
+        buf = cls(a.nbytes)
+        check(buf.lib.lolaCudaCopyToDevice(buf.ptr, a.ctypes.data, a.nbytes), "copy to device")
+        return buf
+
+    def to_array(self, shape, dtype) -> np.ndarray:
+        out = np.empty(shape, dtype)
+        assert out.nbytes <= self.nbytes
+        check(self.lib.lolaCudaCopyToHost(out.ctypes.data, self.ptr, out.nbytes), "copy to host")
+        return out
+
+    def free(self) -> None:
+        if self.ptr:
+            self.lib.lolaCudaDeviceFree(self.ptr)
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+class Plan:
+    """One reconstruction volume on the device plus its projection ring."""
+
+    def __init__(self, n: int, voxel_size: float, origin_index: float, width: int, height: int,
+                 cfg: LolaCudaConfig | None = None, **cfg_kw):
+        self.lib = load_lolacuda()
+        self.n, self.width, self.height = int(n), int(width), int(height)
+        g = LolaCudaGeometry(self.n, self.width, self.height, voxel_size, origin_index)
+        self.cfg = cfg if cfg is not None else config(**cfg_kw)
+        h = C.c_void_p()
+        check(self.lib.lolaCudaPlanCreate(C.byref(g), C.byref(self.cfg), C.byref(h)),
+              "plan create")
+        self.handle = h
+
+    @property
+    def volume_ptr(self) -> int:
+        return self.lib.lolaCudaPlanVolume(self.handle)
+
+    @property
+    def stream(self) -> int:
+        return self.lib.lolaCudaPlanStream(self.handle)
+
+    def zero(self) -> None:
+        check(self.lib.lolaCudaPlanZeroVolume(self.handle), "zero volume")
+
+    def upload(self, vol: np.ndarray) -> None:
+        vol = np.ascontiguousarray(vol, np.float32)
+        assert vol.size == self.n ** 3
+        check(self.lib.lolaCudaPlanUploadVolume(self.handle, vol.ctypes.data), "upload volume")
+
+    def download(self, out: np.ndarray | None = None) -> np.ndarray:
+        if out is None:
+            out = np.empty((self.n, self.n, self.n), np.float32)
+        check(self.lib.lolaCudaPlanDownloadVolume(self.handle, out.ctypes.data), "download")
+        return out
+
+    def backproject_device(self, d_images: int, image_stride: int, matrices: np.ndarray,
+                           count: int | None = None) -> None:
+        m = np.ascontiguousarray(matrices, np.float64).reshape(-1, 12)
+        count = m.shape[0] if count is None else count
+        check(self.lib.lolaCudaPlanBackprojectDevice(self.handle, d_images, image_stride,
+                                                     m.ctypes.data, count), "backproject")
+
+    def backproject_host(self, images: np.ndarray, matrices: np.ndarray) -> None:
+        imgs = np.ascontiguousarray(images, np.float32)
+        m = np.ascontiguousarray(matrices, np.float64).reshape(-1, 12)
+        assert imgs.shape[0] == m.shape[0]
+        stride = self.width * self.height
+        check(self.lib.lolaCudaPlanBackprojectHost(self.handle, imgs.ctypes.data, stride,
+                                                   m.ctypes.data, m.shape[0]), "backproject")
+
+    def synchronize(self) -> None:
+        check(self.lib.lolaCudaPlanSynchronize(self.handle), "synchronize")
+
+    def stats(self) -> LolaCudaStats:
+        s = LolaCudaStats()
+        check(self.lib.lolaCudaPlanGetStats(self.handle, C.byref(s)), "stats")
+        return s
+
+    def reset_stats(self) -> None:
+        check(self.lib.lolaCudaPlanResetStats(self.handle), "reset stats")
+
+    def close(self) -> None:
+        if getattr(self, "handle", None):
+            self.lib.lolaCudaPlanDestroy(self.handle)
+            self.handle = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class GlobalData:
+    """A RabbitCtGlobalData whose buffers are numpy arrays kept alive here."""
+
+    def __init__(self, n: int, voxel_size: float, origin_index: float, width: int, height: int,
+                 batch: int, volume: np.ndarray | None = None,
+                 geometry: np.ndarray | None = None):
+        self.volume = (np.zeros((n, n, n), np.float32) if volume is None else volume)
+        assert self.volume.dtype == np.float32 and self.volume.flags["C_CONTIGUOUS"]
+        self.geometry = None if geometry is None else np.ascontiguousarray(geometry, np.float64)
+        self.mats = np.zeros((batch, 12), np.float64)
+        self.images = np.zeros((batch, height, width), np.float32)
+        self.projs = (Projection * batch)()
+        for i in range(batch):
+            self.projs[i].id = 0
+            self.projs[i].matrix = self.mats[i].ctypes.data_as(C.POINTER(C.c_double))
+            self.projs[i].image = self.images[i].ctypes.data_as(C.POINTER(C.c_float))
+        d = RabbitCtGlobalData()
+        d.problemSize, d.imageWidth, d.imageHeight = n, width, height
+        d.voxelSize, d.O_Index = voxel_size, origin_index
+        d.volumeData = self.volume.ctypes.data_as(C.POINTER(C.c_float))
+        d.numberOfProjections = 0 if self.geometry is None else self.geometry.shape[0]
+        d.globalGeometry = (None if self.geometry is None
+                            else self.geometry.ctypes.data_as(C.POINTER(C.c_double)))
+        d.projectionBuffer = self.projs
+        d.clipFilename = None
+        self.data = d
+
+    @property
+    def ref(self):
+        return C.byref(self.data)
+
+
+def module_functions(lib: C.CDLL, prefix: str):
+    """(prepare, backprojection, finish) of a RabbitCT module in `lib`, e.g.
+    prefix 'lolaCuda' or, for the reference build, 'lolaBunny'."""
+    fns = []
+    for suffix in ("Prepare", "Backprojection", "Finish"):
+        f = getattr(lib, prefix + suffix)
+        f.restype = C.c_int
+        f.argtypes = [C.POINTER(RabbitCtGlobalData)]
+        fns.append(f)
+    return tuple(fns)

@@ -1,0 +1,170 @@
+"""Parity of the CUDA path (through the C ABI) with the FP64 LolaBunny oracle.
+
+Bars (the FP64 oracle is the reference of every comparison):
+  FP32 storage, plain or Kahan       relative RMSE <= 1e-5 (and <= 1e-5 vs the
+                                     FP32-accumulating LolaBunny restatement)
+  FP16 storage (plain or quad)       relative RMSE <= 1e-3
+  BF16 storage (plain or quad)       relative RMSE <= 4e-3 (8-bit mantissa)
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from conftest import small_spec
+from oracle import oracle
+from rabbitct_gb300 import metrics, synth
+
+pytestmark = pytest.mark.gpu
+
+BAR = {"f32": 1e-5, "f32q": 1e-5, "f16": 1e-3, "f16q": 1e-3, "bf16": 4e-3, "bf16q": 4e-3}
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from rabbitct_gb300 import build as b
+    b.build_lolacuda()
+    from rabbitct_gb300._native import load_lolacuda
+    return load_lolacuda()
+
+
+def _scan(**kw):
+    return synth.make_scan(small_spec(**kw))
+
+
+def _geom(n):
+    vs = 256.0 / n
+    return vs, synth.origin_index(n, vs)
+
+
+_cache = {}
+
+
+def _oracle64(scan, n, vs, o):
+    key = (id(scan), n)
+    if key not in _cache:
+        _cache[key] = oracle.bunny_f64(n, vs, o, scan.matrices, scan.images)
+    return _cache[key]
+
+
+@pytest.fixture(scope="module")
+def scan12():
+    return _scan()
+
+
+@pytest.mark.parametrize("storage", ["f32", "f32q", "f16", "f16q", "bf16", "bf16q"])
+@pytest.mark.parametrize("accum", ["plain", "kahan"])
+def test_storage_accum_vs_oracle(lib, scan12, storage, accum):
+    from rabbitct_gb300.lolacuda import Plan
+    n = 48
+    vs, o = _geom(n)
+    ref = _oracle64(scan12, n, vs, o)
+    with Plan(n, vs, o, scan12.width, scan12.height, storage=storage, accumulation=accum,
+              batch=5) as plan:
+        plan.backproject_host(scan12.images, scan12.matrices)
+        vol = plan.download()
+    e = metrics.errors(vol, ref)
+    assert e["rel_rmse"] <= BAR[storage], e
+
+
+@pytest.mark.parametrize("vpt,rows", [(8, 8), (8, 4), (16, 8), (16, 4), (4, 8)])
+@pytest.mark.parametrize("n", [32, 40, 64])
+def test_shapes_and_ragged_sizes(lib, scan12, vpt, rows, n):
+    """Tile shapes, and N that is not a multiple of the tile (ragged edges)."""
+    from rabbitct_gb300.lolacuda import Plan
+    vs, o = _geom(n)
+    ref = _oracle64(scan12, n, vs, o)
+    ref32 = oracle.bunny_f32(n, vs, o, scan12.matrices, scan12.images)
+    with Plan(n, vs, o, scan12.width, scan12.height, storage="f32", batch=7,
+              voxels_per_thread=vpt, rows_per_block=rows) as plan:
+        plan.backproject_host(scan12.images, scan12.matrices)
+        vol = plan.download()
+    assert metrics.errors(vol, ref)["rel_rmse"] <= 1e-5
+    assert metrics.errors(vol, ref32)["rel_rmse"] <= 1e-5
+
+
+@pytest.mark.parametrize("batch", [1, 2, 12, 32])
+def test_batch_sizes_device_path(lib, scan12, batch):
+    """Projections resident in device memory, any pass size."""
+    from rabbitct_gb300.lolacuda import DeviceBuffer, Plan
+    n = 32
+    vs, o = _geom(n)
+    ref = _oracle64(scan12, n, vs, o)
+    d = DeviceBuffer.from_array(scan12.images)
+    with Plan(n, vs, o, scan12.width, scan12.height, storage="f32", batch=batch,
+              collect_stats=1) as plan:
+        plan.backproject_device(d.ptr, scan12.width * scan12.height, scan12.matrices)
+        plan.synchronize()
+        vol = plan.download()
+        st = plan.stats()
+    d.free()
+    assert metrics.errors(vol, ref)["rel_rmse"] <= 1e-5
+    assert st.projections == 12
+    assert st.passes == -(-12 // batch)
+
+
+def test_accumulates_into_initial_volume(lib, scan12):
+    from rabbitct_gb300.lolacuda import Plan
+    n = 32
+    vs, o = _geom(n)
+    rng = np.random.default_rng(0)
+    init = rng.standard_normal((n, n, n)).astype(np.float32) * 1e-4
+    ref = oracle.bunny_f64(n, vs, o, scan12.matrices, scan12.images,
+                           vol=init.astype(np.float64).copy())
+    with Plan(n, vs, o, scan12.width, scan12.height) as plan:
+        plan.upload(init)
+        plan.backproject_host(scan12.images, scan12.matrices)
+        vol = plan.download()
+    assert metrics.errors(vol, ref)["rel_rmse"] <= 1e-5
+
+
+def test_truncation_border_semantics(lib):
+    """A detector much smaller than the volume's shadow: many voxels project
+    to u or v in (-2, 0), where LolaBunny's truncation gives negative weights,
+    and most tiles take the clamped or skipped paths."""
+    from rabbitct_gb300.lolacuda import Plan
+    spec = small_spec(width=64, height=48, nproj=9, seed=21)
+    spec.pitch = 0.308 * 1248 / 64 * 0.5   # half the field of view
+    scan = synth.make_scan(spec)
+    n = 48
+    vs, o = _geom(n)
+    ref = oracle.bunny_f64(n, vs, o, scan.matrices, scan.images)
+    with Plan(n, vs, o, spec.width, spec.height, batch=9, collect_stats=1) as plan:
+        plan.backproject_host(scan.images, scan.matrices)
+        vol = plan.download()
+        st = plan.stats()
+    assert metrics.errors(vol, ref)["rel_rmse"] <= 1e-5
+    assert st.tilePassesSkipped > 0 and st.tilePassesSlow > 0
+
+
+def test_fast_path_exercised(lib):
+    """Full-size detector, N=128: interior tiles run unclamped."""
+    from rabbitct_gb300.lolacuda import Plan
+    spec = synth.ScanSpec(nproj=4, seed=2)
+    scan = synth.make_scan(spec)
+    n = 128
+    vs = synth.voxel_size(n)
+    o = synth.origin_index(n, vs)
+    ref = oracle.bunny_f64(n, vs, o, scan.matrices, scan.images)
+    with Plan(n, vs, o, spec.width, spec.height, batch=4, collect_stats=1) as plan:
+        plan.backproject_host(scan.images, scan.matrices)
+        vol = plan.download()
+        st = plan.stats()
+    assert metrics.errors(vol, ref)["rel_rmse"] <= 1e-5
+    assert st.tilePassesFast > 0
+
+
+@pytest.mark.parametrize("batch_call", [1, 3])
+@pytest.mark.parametrize("with_geometry", [True, False])
+def test_module_api_like_runner(lib, scan12, batch_call, with_geometry):
+    """prepare / backprojection / finish driven like src/rabbitRunner.c."""
+    from rabbitct_gb300._native import config
+    from rabbitct_gb300.lolacuda import module_functions
+    from rabbitct_gb300.runner import run_module
+    n = 40
+    vs, o = _geom(n)
+    ref = _oracle64(scan12, n, vs, o)
+    assert lib.lolaCudaSetConfig(config(storage="f32", batch=5, exit_on_error=0))
+    r = run_module(module_functions(lib, "lolaCuda"), n, vs, o, scan12.matrices, scan12.images,
+                   batch=batch_call, with_geometry=with_geometry)
+    assert metrics.errors(r.volume, ref)["rel_rmse"] <= 1e-5
