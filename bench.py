@@ -1,0 +1,449 @@
+#!/usr/bin/env python3
+"""LolaCUDA benchmark: GUPS of cone-beam backprojection on GB300.
+
+Workload (one step = one full reconstruction): N=1024 volume (0.25 mm voxels,
+4 GiB FP32 resident in HBM), 496 synthetic projections of 1248x960 (seeded
+ellipsoid phantom, circular 200 degree scan) — the RabbitCT dataset's shapes.
+GUPS = N^3 * projections / time (RabbitCT's convention: every voxel counts for
+every projection, clipped or not).
+
+Lines printed (rank 0, one JSON object):
+  value   device-resident throughput of the FP16-stored path (projections
+          already in HBM when the timed region starts; CUDA events on the
+          plan's stream); the FP32 path is measured the same way beside it
+  e2e     the same metric through the RabbitCT module API (prepare, one
+          backprojection call per projection from pinned host buffers,
+          finish with the volume copied back), wall clock around the calls
+  roofline  the pass kernel against the measured gather and FP32-issue
+          ceilings (probe kernels run on the same GPU), plus its HBM view
+  cpu_baseline  the LolaOPT port (oracle/oracle_opt.c) on the host cores,
+          on a bounded sample of the same workload
+`--impl reference` times the reference's CPU method alone (the LolaOPT port;
+the reference's own build cannot travel to this host) on the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+import numpy as np  # noqa: E402
+
+METRIC = "GUPS (1e9 voxel updates/s) N=512,1024: FP16-stored vs FP32 path, RMSE vs FP64"
+
+# Algorithmic instructions per computed voxel update of the pass kernel's
+# method (FP32/INT issue slots): 3 FMA for u,v,w; 1 reciprocal; 2 FMA for the
+# pixel coordinates; 1 mul for 1/w^2; 2 truncations; 2 fraction subtractions;
+# 2 for the stored index (FMA + add) and 1 address; 6 for the two-level
+# bilinear lerp; 1 FMA accumulate = 21, plus the gather loads (4 plain, 1 quad)
+# and the widening of 16-bit taps to FP32 (4 per update).
+INSTR_PER_UPDATE = {"f32": 25, "f16": 29, "bf16": 29, "f32q": 22, "f16q": 26, "bf16q": 26}
+STORAGE_IDS = {"f32": 0, "f16": 1, "bf16": 2, "f32q": 3, "f16q": 4, "bf16q": 5}
+
+
+def parse_args():
+    ap = argparse.ArgumentParser(description=__doc__,
+                                 formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="lolacuda", choices=["lolacuda", "reference"])
+    ap.add_argument("--n", type=int, default=1024)
+    ap.add_argument("--nproj", type=int, default=496)
+    ap.add_argument("--width", type=int, default=1248)
+    ap.add_argument("--height", type=int, default=960)
+    ap.add_argument("--storage", default="f16q", choices=list(STORAGE_IDS))
+    ap.add_argument("--fp32-storage", default="f32", choices=list(STORAGE_IDS))
+    ap.add_argument("--batch", type=int, default=16)
+    ap.add_argument("--vpt", type=int, default=8)
+    ap.add_argument("--rows", type=int, default=8)
+    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--cpu-views", type=int, default=8,
+                    help="projections in the bounded CPU-baseline sample")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-fp32", action="store_true")
+    ap.add_argument("--no-probes", action="store_true")
+    return ap.parse_args()
+
+
+def dist_info():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class Dist:
+    """Host-side barrier and max-reduction across ranks (gloo); no data-path
+    collective: every rank reconstructs its own volume."""
+
+    def __init__(self, rank, world):
+        self.rank, self.world = rank, world
+        self.pg = None
+        if world > 1:
+            import torch.distributed as dist
+            dist.init_process_group("gloo")
+            self.dist = dist
+
+    def barrier(self):
+        if self.world > 1:
+            self.dist.barrier()
+
+    def max(self, x: float) -> float:
+        if self.world == 1:
+            return x
+        import torch
+        t = torch.tensor([x], dtype=torch.float64)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.world > 1:
+            self.dist.destroy_process_group()
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines: list[str] = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.thread.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[4:8]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def make_workload(args):
+    from rabbitct_gb300 import synth
+    spec = synth.ScanSpec(nproj=args.nproj, width=args.width, height=args.height)
+    scan = synth.make_scan(spec)
+    vs = synth.voxel_size(args.n)
+    o = synth.origin_index(args.n, vs)
+    return scan, vs, o
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline: the LolaOPT port on the host cores (bounded sample)
+# ---------------------------------------------------------------------------
+
+def cpu_baseline(args, scan, vs, o, repeats=1) -> dict:
+    from oracle import oracle
+    views = max(1, min(args.cpu_views, scan.nproj))
+    stride = max(1, scan.nproj // views)
+    sel = np.arange(0, stride * views, stride)[:views]
+    mats = scan.matrices[sel]
+    imgs = scan.images[sel]
+    n = args.n
+    # prepare (untimed, like src/rabbitRunner.c:222-232): ranges + padding
+    ob = oracle.OptBaseline(n, vs, o, mats, scan.width, scan.height, vector_size=4)
+    times = []
+    for _ in range(repeats):
+        vol = np.zeros((n, n, n), np.float32)
+        t = 0.0
+        for i in range(views):
+            t0 = time.perf_counter()
+            # one runner call with -b 1; ids index the sampled views' ranges
+            ob.backproject(vol, np.array([i + 1]), imgs[i:i + 1])
+            t += time.perf_counter() - t0
+        times.append(t)
+        del vol
+    gups = [n ** 3 * views / t / 1e9 for t in times]
+    return {"value": statistics.median(gups), "unit": "GUPS", "cores": oracle.threads(),
+            "kind": "port",
+            "sample": (f"LolaOPT port (oracle/oracle_opt.c), {views} of {scan.nproj} "
+                       f"projections at N={n}, one call per projection, OpenMP over "
+                       f"{oracle.threads()} threads"),
+            "per_repeat": gups}
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return 0
+    scan, vs, o = make_workload(args)
+    from oracle import oracle
+    oracle.lib()
+    warm = max(0, args.warmup)
+    # each step: one bounded sample of the workload through the CPU method
+    res = cpu_baseline(args, scan, vs, o, repeats=warm + args.steps)
+    vals = res["per_repeat"][warm:]
+    value = statistics.median(vals)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "GUPS",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": args.n ** 3 * min(args.cpu_views, scan.nproj) / value / 1e6,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded ellipsoid phantom, RabbitCT shapes)",
+        "config": workload_config(args, "f32"),
+        "cpu_baseline": {k: res[k] for k in ("value", "unit", "cores", "kind", "sample")},
+        "e2e": {"value": value, "unit": "GUPS", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+        "note": ("the reference's own compiled modules are built from its sources only where "
+                 "that tree exists; on this host its method runs as the LolaOPT port"),
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def workload_config(args, storage):
+    return {"workload": (f"cone-beam backprojection, N={args.n}^3 FP32 volume, {args.nproj} "
+                         f"projections of {args.width}x{args.height}"),
+            "N": args.n, "projections": args.nproj,
+            "detector": f"{args.width}x{args.height}", "storage": storage,
+            "batch": args.batch, "voxels_per_thread": args.vpt, "rows_per_block": args.rows,
+            "l2": "inputs larger than L2 (volume and projections each exceed 129 MB)",
+            "parallelism": "replicas (one full reconstruction per GPU)"}
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+
+def time_device(args, dist, lib_mod, scan, vs, o, d_images, storage, clocks=None):
+    from rabbitct_gb300.lolacuda import Plan
+    W, H = scan.width, scan.height
+    with Plan(args.n, vs, o, W, H, storage=storage, batch=args.batch,
+              voxels_per_thread=args.vpt, rows_per_block=args.rows, collect_stats=1) as p:
+        for _ in range(args.warmup):
+            p.zero()
+            p.backproject_device(d_images.ptr, W * H, scan.matrices)
+        p.synchronize()
+        p.reset_stats()
+        dist.barrier()
+        p.synchronize()
+        if clocks is not None:
+            clocks.start()
+        p.timer_start()
+        for _ in range(args.steps):
+            p.zero()
+            p.backproject_device(d_images.ptr, W * H, scan.matrices)
+        ms = p.timer_stop()
+        clk = clocks.stop() if clocks is not None else None
+        p.synchronize()
+        dist.barrier()
+        st = p.stats()
+    ms_max = dist.max(ms)
+    updates = float(args.n) ** 3 * scan.nproj * args.steps * dist.world
+    return {"ms": ms_max, "gups": updates / (ms_max * 1e-3) / 1e9, "stats": st, "clocks": clk}
+
+
+def roofline(args, lib, storage, st, probes) -> dict:
+    tile = 32 * args.rows * args.vpt
+    computed = (st.tilePassesFast + st.tilePassesSlow) * tile
+    launches = max(1, st.passes)
+    avg_ms = st.passMs / launches
+    per_launch = computed / launches
+    achieved = per_launch / (avg_ms * 1e-3) / 1e9  # Gupdate/s while the kernel runs
+    out = {"unit": "Gupdate/s", "achieved": achieved, "kernel": "passKernel",
+           "avg_launch_ms": avg_ms, "updates_per_launch": per_launch,
+           "skipped_fraction": st.tilePassesSkipped / max(1, st.tilePassesSkipped +
+                                                           st.tilePassesFast +
+                                                           st.tilePassesSlow)}
+    if probes:
+        issue = probes["issue_inst_per_s"] / INSTR_PER_UPDATE[storage] / 1e9
+        gather = probes["gather"][storage] / 1e9
+        bound, peak = ("issue", issue) if issue <= gather else ("gather", gather)
+        out.update({"bound": bound, "peak": peak, "frac": achieved / peak,
+                    "peak_issue": issue, "peak_gather": gather,
+                    "instr_per_update": INSTR_PER_UPDATE[storage],
+                    "peak_source": "probe kernels on this GPU (lolaCudaProbeIssueRate / "
+                                   "lolaCudaProbeGatherRate)"})
+    # HBM view: volume read + write once per pass plus the stored projections
+    # read once per pass from L2 misses at most (algorithmic floor).
+    elem = {"f32": 4, "f16": 2, "bf16": 2, "f32q": 16, "f16q": 8, "bf16q": 8}[storage]
+    vol_bytes = 8.0 * args.n ** 3
+    proj_bytes = args.batch * (args.width + 128) * (args.height + 128) * elem
+    hbm_gbs = (vol_bytes + proj_bytes) / (avg_ms * 1e-3) / 1e9
+    peaks = {}
+    mp = ROOT / "MEASURED_PEAKS.json"
+    if mp.exists():
+        peaks = json.loads(mp.read_text())
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    out["hbm"] = {"achieved": hbm_gbs, "peak": hbm_peak, "unit": "GB/s",
+                  "frac": hbm_gbs / hbm_peak,
+                  "peak_source": "MEASURED_PEAKS.json" if "hbm_gbs" in peaks else "fallback",
+                  "algorithmic_bytes_per_launch": vol_bytes + proj_bytes}
+    out["traffic"] = None
+    return out
+
+
+def time_e2e(args, dist, scan, vs, o, storage) -> dict:
+    """Module API (prepare / backprojection per projection / finish) with
+    pinned host buffers, as rabbitRunner drives a module with -b 1 -a."""
+    import ctypes as C
+
+    from rabbitct_gb300._native import check, config, load_lolacuda
+    from rabbitct_gb300.lolacuda import GlobalData, module_functions
+    lib = load_lolacuda()
+    n, W, H = args.n, scan.width, scan.height
+    nbytes_vol = 4 * n ** 3
+    nbytes_img = 4 * W * H * scan.nproj
+    hv = lib.lolaCudaHostAlloc(nbytes_vol)
+    hi = lib.lolaCudaHostAlloc(nbytes_img)
+    if not hv or not hi:
+        raise RuntimeError("pinned host allocation failed")
+    vol = np.ctypeslib.as_array((C.c_float * (n ** 3)).from_address(hv)).reshape(n, n, n)
+    imgs = np.ctypeslib.as_array((C.c_float * (W * H * scan.nproj)).from_address(hi))
+    imgs = imgs.reshape(scan.nproj, H, W)
+    imgs[...] = scan.images
+    mats = np.ascontiguousarray(scan.matrices)
+    check(lib.lolaCudaSetConfig(config(storage=storage, batch=args.batch,
+                                       voxels_per_thread=args.vpt, rows_per_block=args.rows,
+                                       exit_on_error=0)), "config")
+    prepare, iterate, finish = module_functions(lib, "lolaCuda")
+    times = []
+    for step in range(1 + args.e2e_steps):
+        vol.fill(0.0)  # the runner hands over a zeroed volume (src/rabbitRunner.c:192)
+        gd = GlobalData(n, vs, o, W, H, 1, volume=vol, geometry=mats)
+        dist.barrier()
+        t0 = time.perf_counter()
+        check(prepare(gd.ref), "prepare")
+        gd.data.numberOfProjections = 1
+        for p in range(scan.nproj):
+            # a zero-copy reader: the projection buffer points at the pinned image
+            gd.projs[0].id = p + 1
+            gd.projs[0].matrix = mats[p].ctypes.data_as(C.POINTER(C.c_double))
+            gd.projs[0].image = C.cast(hi + p * 4 * W * H, C.POINTER(C.c_float))
+            check(iterate(gd.ref), "backprojection")
+        check(finish(gd.ref), "finish")
+        dt = time.perf_counter() - t0
+        dist.barrier()
+        if step > 0:
+            times.append(dist.max(dt))
+    checksum = float(np.float64(vol[n // 2].sum()))
+    lib.lolaCudaHostFree(hv)
+    lib.lolaCudaHostFree(hi)
+    t = statistics.median(times)
+    gups = float(n) ** 3 * scan.nproj * dist.world / t / 1e9
+    return {"value": gups, "unit": "GUPS", "seconds": t,
+            "h2d_bytes_per_step": nbytes_vol + nbytes_img,
+            "d2h_bytes_per_step": nbytes_vol, "path": "module API, -b 1 calls, pinned host",
+            "checksum_mid_slice": checksum}
+
+
+def run_gpu(args, rank, world, local):
+    if world > 1 and "CUDA_VISIBLE_DEVICES" not in os.environ:
+        os.environ["CUDA_VISIBLE_DEVICES"] = str(local)
+    dist = Dist(rank, world)
+    from rabbitct_gb300 import build as b
+    b.build_lolacuda()
+    b.build_synth()
+    from rabbitct_gb300._native import load_lolacuda
+    from rabbitct_gb300.lolacuda import DeviceBuffer
+    lib = load_lolacuda()
+    scan, vs, o = make_workload(args)
+    d_images = DeviceBuffer.from_array(scan.images)
+
+    probes = None
+    if not args.no_probes:
+        probes = {"issue_inst_per_s": lib.lolaCudaProbeIssueRate(),
+                  "gather": {s: lib.lolaCudaProbeGatherRate(STORAGE_IDS[s], scan.width,
+                                                            scan.height)
+                             for s in {args.storage, args.fp32_storage}}}
+
+    clocks = ClockSampler(0)
+    head = time_device(args, dist, lib, scan, vs, o, d_images, args.storage, clocks)
+    fp32 = None
+    if not args.no_fp32 and args.fp32_storage != args.storage:
+        fp32 = time_device(args, dist, lib, scan, vs, o, d_images, args.fp32_storage)
+    d_images.free()
+    e2e = None if args.no_e2e else time_e2e(args, dist, scan, vs, o, args.storage)
+
+    if rank != 0:
+        dist.close()
+        return 0
+    st = head["stats"]
+    line = {
+        "metric": METRIC, "value": head["gups"], "unit": "GUPS", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": head["ms"] / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded ellipsoid phantom, RabbitCT shapes)",
+        "config": workload_config(args, args.storage),
+        "gpu_launches": int(st.passes + st.packs),
+        "clocks": head["clocks"],
+        "roofline": roofline(args, lib, args.storage, st, probes),
+    }
+    if fp32 is not None:
+        line["fp32_path"] = {"value": fp32["gups"], "unit": "GUPS",
+                             "storage": args.fp32_storage,
+                             "ms_per_step": fp32["ms"] / args.steps,
+                             "roofline": roofline(args, lib, args.fp32_storage, fp32["stats"],
+                                                  probes)}
+        line["fp16_over_fp32"] = head["gups"] / fp32["gups"]
+    if e2e is not None:
+        line["e2e"] = e2e
+    if probes:
+        line["probes"] = probes
+    if world == 1 and not args.no_cpu:
+        line["cpu_baseline"] = {k: v for k, v in cpu_baseline(args, scan, vs, o).items()
+                                if k != "per_repeat"}
+    print(json.dumps(line), flush=True)
+    dist.close()
+    return 0
+
+
+def main():
+    args = parse_args()
+    rank, world, local = dist_info()
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+    return run_gpu(args, rank, world, local)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

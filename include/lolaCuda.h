@@ -172,6 +172,11 @@ int lolaCudaPlanBackprojectHost(LolaCudaPlan *plan, const float *h_images,
     size_t imageStride, const double *h_matrices, int count);
 
 int lolaCudaPlanSynchronize(LolaCudaPlan *plan);
+
+/* CUDA-event timer on the plan's stream: Start records an event, Stop records
+ * one, waits for it and returns the elapsed milliseconds in *ms. */
+int lolaCudaPlanTimerStart(LolaCudaPlan *plan);
+int lolaCudaPlanTimerStop(LolaCudaPlan *plan, double *ms);
 int lolaCudaPlanGetStats(LolaCudaPlan *plan, LolaCudaStats *stats);
 int lolaCudaPlanResetStats(LolaCudaPlan *plan);
 
@@ -182,6 +187,20 @@ int lolaCudaDeviceFree(void *d_ptr);
 int lolaCudaCopyToDevice(void *d_dst, const void *h_src, size_t bytes);
 int lolaCudaCopyToHost(void *h_dst, const void *d_src, size_t bytes);
 int lolaCudaDeviceSynchronize(void);
+
+/* Page-locked host memory (cudaHostAlloc), so callers' projection and volume
+ * buffers can be DMA'd at full link speed. */
+void *lolaCudaHostAlloc(size_t bytes);
+int lolaCudaHostFree(void *h_ptr);
+
+/* ---- Measurement helpers (used by the benchmark's roofline) ----------------
+ * FP32 FMA issue rate of the current device, thread-instructions per second. */
+double lolaCudaProbeIssueRate(void);
+/* Voxel updates per second that the pass kernel's 2x2 gather pattern alone
+ * sustains for a storage layout over a padded width x height detector. */
+double lolaCudaProbeGatherRate(int storage, int width, int height);
+/* SM count, SM clock (kHz) and name of the current device. */
+int lolaCudaDeviceInfo(int *smCount, int *clockKHz, char *name, int nameLen);
 
 #ifdef __cplusplus
 }

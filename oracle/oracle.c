@@ -163,14 +163,19 @@ static inline int voxelHits(const double *a, double x, double y, double z, int W
 void oracleLineRanges(int N, float voxelSize, float originIndex, int W, int H, int nproj,
     const double *mats, int vectorSize, int signedHit, int16_t *ranges)
 {
-#pragma omp parallel for schedule(dynamic, 1)
+  /* the reference steps wz / wy as float accumulators (wz += mm); the same
+     sequence is precomputed so rows can be scanned in parallel */
+  float *wseq = (float *)malloc((size_t)N * sizeof(float));
+  float acc = originIndex;
+  for (int i = 0; i < N; i++, acc += voxelSize)
+    wseq[i] = acc;
+#pragma omp parallel for schedule(dynamic, 4) collapse(2)
   for (int p = 0; p < nproj; p++) {
-    const double *a = mats + 12 * (size_t)p;
-    /* the reference steps wz / wy as float accumulators (wz += mm) */
-    float wz = originIndex;
-    for (int z = 0; z < N; z++, wz += voxelSize) {
-      float wy = originIndex;
-      for (int y = 0; y < N; y++, wy += voxelSize) {
+    for (int z = 0; z < N; z++) {
+      const double *a = mats + 12 * (size_t)p;
+      const float wz = wseq[z];
+      for (int y = 0; y < N; y++) {
+        const float wy = wseq[y];
         int xstart = -1, xstop = -1;
         for (int x = 0; x < N; x++) {
           const float wx = x * voxelSize + originIndex;
@@ -202,6 +207,7 @@ void oracleLineRanges(int N, float voxelSize, float originIndex, int W, int H, i
       }
     }
   }
+  free(wseq);
 }
 
 /* Number of threads OpenMP would use (1 without OpenMP). */

@@ -94,6 +94,8 @@ _SIGNATURES = [
     ("lolaCudaPlanBackprojectDevice", C.c_int, [_P, _P, C.c_size_t, _P, C.c_int]),
     ("lolaCudaPlanBackprojectHost", C.c_int, [_P, _P, C.c_size_t, _P, C.c_int]),
     ("lolaCudaPlanSynchronize", C.c_int, [_P]),
+    ("lolaCudaPlanTimerStart", C.c_int, [_P]),
+    ("lolaCudaPlanTimerStop", C.c_int, [_P, C.POINTER(C.c_double)]),
     ("lolaCudaPlanGetStats", C.c_int, [_P, C.POINTER(LolaCudaStats)]),
     ("lolaCudaPlanResetStats", C.c_int, [_P]),
     ("lolaCudaDeviceAlloc", _P, [C.c_size_t]),
@@ -101,6 +103,12 @@ _SIGNATURES = [
     ("lolaCudaCopyToDevice", C.c_int, [_P, _P, C.c_size_t]),
     ("lolaCudaCopyToHost", C.c_int, [_P, _P, C.c_size_t]),
     ("lolaCudaDeviceSynchronize", C.c_int, []),
+    ("lolaCudaHostAlloc", _P, [C.c_size_t]),
+    ("lolaCudaHostFree", C.c_int, [_P]),
+    ("lolaCudaProbeIssueRate", C.c_double, []),
+    ("lolaCudaProbeGatherRate", C.c_double, [C.c_int, C.c_int, C.c_int]),
+    ("lolaCudaDeviceInfo", C.c_int, [C.POINTER(C.c_int), C.POINTER(C.c_int), C.c_char_p,
+                                     C.c_int]),
 ]
 
 _lola = None

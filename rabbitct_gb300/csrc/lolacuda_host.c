@@ -161,6 +161,7 @@ struct LolaCudaPlan {
   cudaStream_t copyStream;  /* host uploads into the stage */
   cudaEvent_t stageFree;    /* stage consumed by the last pack */
   cudaEvent_t stageReady;   /* uploads of the pending batch done */
+  cudaEvent_t timerStart, timerStop;
   float *d_volume;
   void *d_ring;
   float *d_stage;
@@ -210,6 +211,10 @@ static int planRelease(LolaCudaPlan *p)
     cudaEventDestroy(p->stageFree);
   if (p->stageReady)
     cudaEventDestroy(p->stageReady);
+  if (p->timerStart)
+    cudaEventDestroy(p->timerStart);
+  if (p->timerStop)
+    cudaEventDestroy(p->timerStop);
   if (p->stream)
     cudaStreamDestroy(p->stream);
   if (p->copyStream)
@@ -231,6 +236,8 @@ static int planInit(LolaCudaPlan *p)
   CUDA_TRY(cudaStreamCreateWithFlags(&p->copyStream, cudaStreamNonBlocking));
   CUDA_TRY(cudaEventCreateWithFlags(&p->stageFree, cudaEventDisableTiming));
   CUDA_TRY(cudaEventCreateWithFlags(&p->stageReady, cudaEventDisableTiming));
+  CUDA_TRY(cudaEventCreate(&p->timerStart));
+  CUDA_TRY(cudaEventCreate(&p->timerStop));
 
   LolaStoreDesc *s = &p->store;
   s->storage = p->cfg.storage;
@@ -494,6 +501,28 @@ int lolaCudaPlanSynchronize(LolaCudaPlan *p)
     return 0;
   CUDA_TRY(cudaStreamSynchronize(p->copyStream));
   CUDA_TRY(cudaStreamSynchronize(p->stream));
+  return 1;
+}
+
+int lolaCudaPlanTimerStart(LolaCudaPlan *p)
+{
+  if (p == NULL)
+    return setError("null plan");
+  CUDA_TRY(cudaSetDevice(p->device));
+  CUDA_TRY(cudaEventRecord(p->timerStart, p->stream));
+  return 1;
+}
+
+int lolaCudaPlanTimerStop(LolaCudaPlan *p, double *ms)
+{
+  if (p == NULL || ms == NULL)
+    return setError("null argument");
+  CUDA_TRY(cudaSetDevice(p->device));
+  CUDA_TRY(cudaEventRecord(p->timerStop, p->stream));
+  CUDA_TRY(cudaEventSynchronize(p->timerStop));
+  float f = 0.0f;
+  CUDA_TRY(cudaEventElapsedTime(&f, p->timerStart, p->timerStop));
+  *ms = (double)f;
   return 1;
 }
 

@@ -1,0 +1,205 @@
+/* Roofline probes: the two throughputs that bound the backprojection pass.
+ *
+ *  issue   independent FP32 FMA chains, the SM's FP32 instruction issue rate
+ *          (thread-instructions / s).  The pass kernel is a chain of FP32 and
+ *          integer ops per voxel update, so issue rate / (instructions per
+ *          update) bounds its update rate.
+ *  gather  the pass kernel's local 2D gather pattern with trivial arithmetic:
+ *          each warp reads, for 32 lanes at detector columns spaced 1.25 px
+ *          apart, the 2x2 taps of an L2-resident stored projection, in the
+ *          kernel's storage layouts (4 x 4 B, 4 x 2 B, 1 x 16 B or 1 x 8 B per
+ *          update).  Returns updates / s the gather path alone sustains.
+ * Both run on every SM with enough warps to saturate it and are timed with
+ * CUDA events on the caller's stream.
+ */
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "lolaCuda.h"
+
+namespace {
+
+__global__ void __launch_bounds__(256) issueProbe(float *out, int iters, float a, float b)
+{
+  float x0 = threadIdx.x * 1e-3f, x1 = x0 + 1.f, x2 = x0 + 2.f, x3 = x0 + 3.f;
+  float x4 = x0 + 4.f, x5 = x0 + 5.f, x6 = x0 + 6.f, x7 = x0 + 7.f;
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      x0 = fmaf(x0, a, b);
+      x1 = fmaf(x1, a, b);
+      x2 = fmaf(x2, a, b);
+      x3 = fmaf(x3, a, b);
+      x4 = fmaf(x4, a, b);
+      x5 = fmaf(x5, a, b);
+      x6 = fmaf(x6, a, b);
+      x7 = fmaf(x7, a, b);
+    }
+  }
+  const float s = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+  if (s == 1234.5f)
+    out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
+/* kind: 0 = 4 x FP32 taps, 1 = 4 x 16-bit taps, 2 = 1 x 16 B quad, 3 = 1 x 8 B quad */
+template <int KIND>
+__global__ void __launch_bounds__(256) gatherProbe(const void *img, int pitch, int rows,
+    int iters, float *out)
+{
+  const int lane = threadIdx.x & 31;
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  /* columns 1.25 px apart across the warp, as adjacent voxels project */
+  const uint32_t span = (uint32_t)(pitch - 64) * (uint32_t)(rows - 2);
+  uint32_t state = 2654435761u * (uint32_t)(warp + 1);
+  float acc = 0.0f;
+  for (int i = 0; i < iters; ++i) {
+    state = state * 1664525u + 1013904223u;
+    const uint32_t base = (state >> 8) % span;
+    const uint32_t idx = base + ((uint32_t)lane * 5u >> 2);
+    if (KIND == 0) {
+      const float *f = static_cast<const float *>(img) + idx;
+      acc += __ldg(f) + __ldg(f + 1) + __ldg(f + pitch) + __ldg(f + pitch + 1);
+    } else if (KIND == 1) {
+      const unsigned short *h = static_cast<const unsigned short *>(img) + idx;
+      acc += __uint_as_float(((uint32_t)__ldg(h) << 16) | __ldg(h + 1)) +
+             __uint_as_float(((uint32_t)__ldg(h + pitch) << 16) | __ldg(h + pitch + 1));
+    } else if (KIND == 2) {
+      const float4 q = __ldg(static_cast<const float4 *>(img) + idx);
+      acc += (q.x + q.y) + (q.z + q.w);
+    } else {
+      const uint2 q = __ldg(static_cast<const uint2 *>(img) + idx);
+      acc += __uint_as_float(q.x) + __uint_as_float(q.y);
+    }
+  }
+  if (acc == 1234.5f)
+    out[0] = acc;
+}
+
+int smCount()
+{
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  return sms;
+}
+
+} /* namespace */
+
+/* Thread-level FP32 FMA instructions per second. */
+extern "C" double lolaCudaProbeIssueRate(void)
+{
+  const int sms = smCount();
+  const int blocks = sms * 8, threads = 256, iters = 4096;
+  float *out = nullptr;
+  if (cudaMalloc(&out, (size_t)blocks * threads * sizeof(float)) != cudaSuccess)
+    return -1.0;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  issueProbe<<<blocks, threads>>>(out, 64, 0.999f, 1e-3f);
+  cudaEventRecord(e0);
+  issueProbe<<<blocks, threads>>>(out, iters, 0.999f, 1e-3f);
+  cudaEventRecord(e1);
+  cudaEventSynchronize(e1);
+  float ms = 0.0f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(out);
+  if (cudaGetLastError() != cudaSuccess || ms <= 0.0f)
+    return -1.0;
+  const double fmas = (double)blocks * threads * iters * 64.0;
+  return fmas / (ms * 1e-3);
+}
+
+/* Voxel updates per second the gather alone sustains, for a storage layout
+ * (LOLA_STORE_*) over a width x height detector padded like the pass kernel. */
+extern "C" double lolaCudaProbeGatherRate(int storage, int width, int height)
+{
+  const int pitch = width + 128, rows = height + 128;
+  int kind, elem;
+  switch (storage) {
+  case LOLA_STORE_F32: kind = 0; elem = 4; break;
+  case LOLA_STORE_F16:
+  case LOLA_STORE_BF16: kind = 1; elem = 2; break;
+  case LOLA_STORE_F32Q: kind = 2; elem = 16; break;
+  case LOLA_STORE_F16Q:
+  case LOLA_STORE_BF16Q: kind = 3; elem = 8; break;
+  default: return -1.0;
+  }
+  const size_t bytes = (size_t)pitch * rows * elem;
+  void *img = nullptr;
+  float *out = nullptr;
+  if (cudaMalloc(&img, bytes) != cudaSuccess)
+    return -1.0;
+  if (cudaMalloc(&out, sizeof(float)) != cudaSuccess) {
+    cudaFree(img);
+    return -1.0;
+  }
+  cudaMemset(img, 0, bytes);
+  const int sms = smCount();
+  const int blocks = sms * 8, threads = 256, iters = 2048;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  auto launch = [&](int it) {
+    switch (kind) {
+    case 0: gatherProbe<0><<<blocks, threads>>>(img, pitch, rows, it, out); break;
+    case 1: gatherProbe<1><<<blocks, threads>>>(img, pitch, rows, it, out); break;
+    case 2: gatherProbe<2><<<blocks, threads>>>(img, pitch, rows, it, out); break;
+    default: gatherProbe<3><<<blocks, threads>>>(img, pitch, rows, it, out); break;
+    }
+  };
+  launch(64);
+  cudaEventRecord(e0);
+  launch(iters);
+  cudaEventRecord(e1);
+  cudaEventSynchronize(e1);
+  float ms = 0.0f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(img);
+  cudaFree(out);
+  if (cudaGetLastError() != cudaSuccess || ms <= 0.0f)
+    return -1.0;
+  return (double)blocks * threads * iters / (ms * 1e-3);
+}
+
+extern "C" int lolaCudaDeviceInfo(int *smCountOut, int *clockKHz, char *name, int nameLen)
+{
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess)
+    return 0;
+  cudaDeviceProp prop;
+  if (cudaGetDeviceProperties(&prop, dev) != cudaSuccess)
+    return 0;
+  if (smCountOut)
+    *smCountOut = prop.multiProcessorCount;
+  if (clockKHz) {
+    int c = 0;
+    cudaDeviceGetAttribute(&c, cudaDevAttrClockRate, dev);
+    *clockKHz = c;
+  }
+  if (name && nameLen > 0) {
+    int i = 0;
+    for (; i < nameLen - 1 && prop.name[i]; i++)
+      name[i] = prop.name[i];
+    name[i] = 0;
+  }
+  return 1;
+}
+
+extern "C" void *lolaCudaHostAlloc(size_t bytes)
+{
+  void *p = nullptr;
+  if (cudaHostAlloc(&p, bytes, cudaHostAllocDefault) != cudaSuccess)
+    return nullptr;
+  return p;
+}
+
+extern "C" int lolaCudaHostFree(void *p)
+{
+  return cudaFreeHost(p) == cudaSuccess;
+}

@@ -105,6 +105,15 @@ class Plan:
     def synchronize(self) -> None:
         check(self.lib.lolaCudaPlanSynchronize(self.handle), "synchronize")
 
+    def timer_start(self) -> None:
+        check(self.lib.lolaCudaPlanTimerStart(self.handle), "timer start")
+
+    def timer_stop(self) -> float:
+        """Milliseconds since timer_start, measured by CUDA events on the plan stream."""
+        ms = C.c_double()
+        check(self.lib.lolaCudaPlanTimerStop(self.handle, C.byref(ms)), "timer stop")
+        return ms.value
+
     def stats(self) -> LolaCudaStats:
         s = LolaCudaStats()
         check(self.lib.lolaCudaPlanGetStats(self.handle, C.byref(s)), "stats")
