@@ -180,6 +180,29 @@ int lolaCudaPlanTimerStop(LolaCudaPlan *plan, double *ms);
 int lolaCudaPlanGetStats(LolaCudaPlan *plan, LolaCudaStats *stats);
 int lolaCudaPlanResetStats(LolaCudaPlan *plan);
 
+/* ---- Backprojection without device allocation ------------------------------
+ * No counterpart in the reference (its modules are CPU code).  For callers
+ * that cannot allocate device memory while they run — an acquisition loop
+ * that reserves its device memory at start-up and must not stall on
+ * cudaMalloc/cudaFree (which can synchronise the device), or a host framework
+ * that owns the device memory pool.  Same result as lolaCudaPlanBackprojectDevice
+ * into a caller-owned volume: d_volume (N^3 FP32, x fastest) += the `count`
+ * FP32 projections at d_images[p * imageStride + j * W + i] with host matrices
+ * h_matrices[p * 12 + ...].  Enqueued on `stream` (a cudaStream_t, NULL = the
+ * default stream); the caller synchronises.  `config` may be NULL (defaults);
+ * its batch is capped by what fits in the scratch.
+ * Calls no cudaMalloc, cudaFree or other allocating routine: the packed
+ * projections live in a fixed LOLA_NOALLOC_SCRATCH_BYTES device array that
+ * every GPU loading this library holds until exit.  A packed projection larger
+ * than that array is rejected with an error.  All calls share the array, so
+ * calls whose work overlaps on the GPU race and must be serialised.  The
+ * array's device address is looked up on the first call on each device: make
+ * that call before any stream capture begins. */
+#define LOLA_NOALLOC_SCRATCH_BYTES (32u << 20)
+int lolaCudaBackprojectNoAlloc(const LolaCudaGeometry *geometry, const LolaCudaConfig *config,
+    float *d_volume, const float *d_images, size_t imageStride, const double *h_matrices,
+    int count, void *stream);
+
 /* Small device-memory helpers so hosts without a CUDA binding (ctypes, cgo)
  * can stage device-resident inputs. */
 void *lolaCudaDeviceAlloc(size_t bytes);

@@ -103,6 +103,9 @@ _SIGNATURES = [
     ("lolaCudaCopyToDevice", C.c_int, [_P, _P, C.c_size_t]),
     ("lolaCudaCopyToHost", C.c_int, [_P, _P, C.c_size_t]),
     ("lolaCudaDeviceSynchronize", C.c_int, []),
+    ("lolaCudaBackprojectNoAlloc", C.c_int, [C.POINTER(LolaCudaGeometry),
+                                             C.POINTER(LolaCudaConfig), _P, _P, C.c_size_t,
+                                             _P, C.c_int, _P]),
     ("lolaCudaHostAlloc", _P, [C.c_size_t]),
     ("lolaCudaHostFree", C.c_int, [_P]),
     ("lolaCudaProbeIssueRate", C.c_double, []),

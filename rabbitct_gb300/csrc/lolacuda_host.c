@@ -43,6 +43,15 @@ const char *lolaCudaLastError(void)
   return gLastError;
 }
 
+int lolaSetError(const char *fmt, ...)
+{
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(gLastError, sizeof(gLastError), fmt, ap);
+  va_end(ap);
+  return 0;
+}
+
 #define CUDA_TRY(call)                                                                   \
   do {                                                                                   \
     cudaError_t e_ = (call);                                                             \

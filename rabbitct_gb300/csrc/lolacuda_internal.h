@@ -59,6 +59,9 @@ int lolaLaunchPack(const LolaStoreDesc *store, const float *d_src, size_t srcStr
 int lolaLaunchBackproject(const LolaStoreDesc *store, const LolaPassParams *params,
     const void *d_ring, float *d_volume, unsigned long long *d_tileCounters, void *stream);
 
+/* Sets the thread's lolaCudaLastError() message; returns 0. */
+int lolaSetError(const char *fmt, ...);
+
 /* 1 if the (voxelsPerThread, rowsPerBlock) pair has a compiled kernel. */
 int lolaKernelShapeSupported(int voxelsPerThread, int rowsPerBlock);
 

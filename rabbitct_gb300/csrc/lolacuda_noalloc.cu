@@ -1,0 +1,172 @@
+/* Backprojection without device allocation.
+ *
+ * Some callers cannot allocate device memory while they run: an acquisition
+ * loop that reserves all of its device memory at start-up and must not stall
+ * on cudaMalloc / cudaFree (both can synchronise the whole device), or a host
+ * framework that owns the device memory pool and forbids libraries from
+ * allocating behind its back.  lolaCudaBackprojectNoAlloc serves them: the
+ * caller passes the volume and the projections, already in device memory, and
+ * the only scratch the operation needs — the ring of packed, zero-padded
+ * projections that the pass kernel gathers from — is the fixed array below,
+ * part of the library's device image.
+ *
+ * Limits and sharing:
+ *  - the scratch is LOLA_NOALLOC_SCRATCH_BYTES (32 MiB) on every GPU that
+ *    loads the library, held until the process exits;
+ *  - one packed projection must fit in it (for FP32 storage about 6 MB at
+ *    1248x960); as many as fit, up to the configured batch, share a pass;
+ *  - every call uses the same array.  The pack kernel rewrites every element
+ *    of each ring slot, zero margin included, before a pass reads it, so no
+ *    state carries over from the previous call; but two calls whose work
+ *    overlaps on the GPU (different streams, or different host threads on one
+ *    device) race on the array and must be serialised by the caller.
+ *  - the device address of the array is looked up once per device, on the
+ *    first call made with that device current; make that first call before
+ *    any stream capture begins.
+ */
+#include <mutex>
+
+#include <cuda_runtime.h>
+
+#include "lolaCuda.h"
+#include "lolacuda_internal.h"
+
+static __device__ __align__(256) unsigned char gNoAllocScratch[LOLA_NOALLOC_SCRATCH_BYTES];
+
+namespace {
+
+constexpr int kMaxDevices = 64;
+void *gScratchAddr[kMaxDevices];
+std::mutex gScratchMutex;
+
+/* Device address of gNoAllocScratch on `device` (the current device).  The
+ * symbol's name in host code is only a host-side handle, so the address must
+ * come from the runtime. */
+int scratchAddress(int device, void **out)
+{
+  if (device < 0 || device >= kMaxDevices)
+    return lolaSetError("device ordinal %d above %d", device, kMaxDevices - 1);
+  std::lock_guard<std::mutex> lock(gScratchMutex);
+  if (gScratchAddr[device] == nullptr) {
+    void *p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, gNoAllocScratch);
+    if (e != cudaSuccess)
+      return lolaSetError("cudaGetSymbolAddress(no-alloc scratch): %s", cudaGetErrorString(e));
+    gScratchAddr[device] = p;
+  }
+  *out = gScratchAddr[device];
+  return 1;
+}
+
+int elemBytes(int storage)
+{
+  switch (storage) {
+  case LOLA_STORE_F32: return 4;
+  case LOLA_STORE_F16:
+  case LOLA_STORE_BF16: return 2;
+  case LOLA_STORE_F32Q: return 16;
+  case LOLA_STORE_F16Q:
+  case LOLA_STORE_BF16Q: return 8;
+  default: return 0;
+  }
+}
+
+} /* namespace */
+
+extern "C" int lolaCudaBackprojectNoAlloc(const LolaCudaGeometry *g, const LolaCudaConfig *config,
+    float *d_volume, const float *d_images, size_t imageStride, const double *h_matrices,
+    int count, void *stream)
+{
+  if (g == nullptr)
+    return lolaSetError("null geometry");
+  LolaCudaConfig c;
+  if (config != nullptr)
+    c = *config;
+  else
+    lolaCudaDefaultConfig(&c);
+  if (count < 0)
+    return lolaSetError("negative projection count");
+  if (g->problemSize <= 0 || g->problemSize > 2048 || g->imageWidth <= 0 || g->imageHeight <= 0)
+    return lolaSetError("invalid geometry N=%d W=%d H=%d", g->problemSize, g->imageWidth,
+        g->imageHeight);
+  if (!(g->voxelSize > 0.0f))
+    return lolaSetError("voxel size must be positive");
+  const int eb = elemBytes(c.storage);
+  if (eb == 0)
+    return lolaSetError("invalid storage %d", c.storage);
+  if (c.accumulation != LOLA_ACCUM_PLAIN && c.accumulation != LOLA_ACCUM_KAHAN)
+    return lolaSetError("invalid accumulation %d", c.accumulation);
+  if (!lolaKernelShapeSupported(c.voxelsPerThread, c.rowsPerBlock))
+    return lolaSetError("no kernel for %d voxels per thread x %d rows per block",
+        c.voxelsPerThread, c.rowsPerBlock);
+  if (count == 0)
+    return 1;
+  if (d_volume == nullptr || d_images == nullptr || h_matrices == nullptr)
+    return lolaSetError("null argument");
+
+  LolaStoreDesc st;
+  st.storage = c.storage;
+  st.elemBytes = eb;
+  st.margin = LOLA_MARGIN;
+  st.width = g->imageWidth;
+  st.height = g->imageHeight;
+  st.pitch = g->imageWidth + 2 * LOLA_MARGIN;
+  st.rows = g->imageHeight + 2 * LOLA_MARGIN;
+  st.reserved = 0;
+  if ((long long)st.pitch * st.rows >= (1LL << 23) - 2 * (long long)st.pitch)
+    return lolaSetError("detector %dx%d too large (padded image must stay below 2^23 pixels)",
+        g->imageWidth, g->imageHeight);
+  st.slotElems = ((size_t)st.pitch * (size_t)st.rows + 63) & ~(size_t)63;
+  const size_t slotBytes = st.slotElems * (size_t)eb;
+  if (slotBytes > LOLA_NOALLOC_SCRATCH_BYTES)
+    return lolaSetError("one packed %dx%d projection needs %zu bytes; the no-allocation "
+                        "entry point has %u bytes of scratch (use FP16/BF16 or plain "
+                        "storage, or the plan API)",
+        g->imageWidth, g->imageHeight, slotBytes, (unsigned)LOLA_NOALLOC_SCRATCH_BYTES);
+  int perPass = (int)(LOLA_NOALLOC_SCRATCH_BYTES / slotBytes);
+  if (perPass > LOLA_MAX_BATCH)
+    perPass = LOLA_MAX_BATCH;
+  if (c.batch >= 1 && perPass > c.batch)
+    perPass = c.batch;
+
+  int device = 0;
+  cudaError_t e = cudaGetDevice(&device);
+  if (e != cudaSuccess)
+    return lolaSetError("cudaGetDevice: %s", cudaGetErrorString(e));
+  void *ring = nullptr;
+  if (!scratchAddress(device, &ring))
+    return 0;
+
+  LolaPassParams P;
+  for (int done = 0; done < count;) {
+    const int n = (count - done < perPass) ? count - done : perPass;
+    int rc = lolaLaunchPack(&st, d_images + (size_t)done * imageStride, imageStride, ring, 0, n,
+        stream);
+    if (rc != 0)
+      return lolaSetError("pack launch failed: %s", cudaGetErrorString((cudaError_t)rc));
+    P.N = g->problemSize;
+    P.count = n;
+    P.voxelSize = g->voxelSize;
+    P.originIndex = g->originIndex;
+    P.accumulation = c.accumulation;
+    P.voxelsPerThread = c.voxelsPerThread;
+    P.rowsPerBlock = c.rowsPerBlock;
+    P.countTiles = 0;
+    for (int i = 0; i < n; i++) {
+      const double *m = h_matrices + 12 * (size_t)(done + i);
+      LolaPassProj &pp = P.proj[i];
+      for (int k = 0; k < 12; k++)
+        pp.a[k] = m[k];
+      for (int ax = 0; ax < 3; ax++)
+        for (int comp = 0; comp < 3; comp++)
+          pp.step[ax][comp] = (float)(m[ax * 3 + comp] * (double)g->voxelSize);
+      pp.slot = i;
+      pp.reserved[0] = pp.reserved[1] = pp.reserved[2] = 0;
+    }
+    rc = lolaLaunchBackproject(&st, &P, ring, d_volume, nullptr, stream);
+    if (rc != 0)
+      return lolaSetError("pass launch failed: %s", cudaGetErrorString((cudaError_t)rc));
+    done += n;
+  }
+  return 1;
+}
