@@ -46,9 +46,13 @@ METRIC = "GUPS (1e9 voxel updates/s) N=512,1024: FP16-stored vs FP32 path, RMSE 
 # pixel coordinates; 1 mul for 1/w^2; 2 truncations; 2 fraction subtractions;
 # 2 for the stored index (FMA + add) and 1 address; 6 for the two-level
 # bilinear lerp; 1 FMA accumulate = 21, plus the gather loads (4 plain, 1 quad)
-# and the widening of 16-bit taps to FP32 (4 per update).
-INSTR_PER_UPDATE = {"f32": 25, "f16": 29, "bf16": 29, "f32q": 22, "f16q": 26, "bf16q": 26}
-STORAGE_IDS = {"f32": 0, "f16": 1, "bf16": 2, "f32q": 3, "f16q": 4, "bf16q": 5}
+# and the widening of 16-bit taps to FP32 (4 per update).  The texture layouts
+# replace the index, address and widening work by 2 coordinate adds and one
+# 4-texel gather.
+INSTR_PER_UPDATE = {"f32": 25, "f16": 29, "bf16": 29, "f32q": 22, "f16q": 26, "bf16q": 26,
+                    "tex32": 21, "tex16": 21}
+STORAGE_IDS = {"f32": 0, "f16": 1, "bf16": 2, "f32q": 3, "f16q": 4, "bf16q": 5, "tex32": 6,
+               "tex16": 7}
 
 
 def parse_args():
@@ -304,7 +308,8 @@ def roofline(args, lib, storage, st, probes) -> dict:
                                    "lolaCudaProbeGatherRate)"})
     # HBM view: volume read + write once per pass plus the stored projections
     # read once per pass from L2 misses at most (algorithmic floor).
-    elem = {"f32": 4, "f16": 2, "bf16": 2, "f32q": 16, "f16q": 8, "bf16q": 8}[storage]
+    elem = {"f32": 4, "f16": 2, "bf16": 2, "f32q": 16, "f16q": 8, "bf16q": 8, "tex32": 4,
+            "tex16": 2}[storage]
     vol_bytes = 8.0 * args.n ** 3
     proj_bytes = args.batch * (args.width + 128) * (args.height + 128) * elem
     hbm_gbs = (vol_bytes + proj_bytes) / (avg_ms * 1e-3) / 1e9

@@ -89,7 +89,9 @@ enum {
   LOLA_STORE_BF16 = 2,  /* 4 BF16 taps */
   LOLA_STORE_F32Q = 3,  /* FP32, 2x2 neighbourhood packed per pixel: 1 x 16 B load */
   LOLA_STORE_F16Q = 4,  /* FP16, packed 2x2: 1 x 8 B load */
-  LOLA_STORE_BF16Q = 5  /* BF16, packed 2x2: 1 x 8 B load */
+  LOLA_STORE_BF16Q = 5, /* BF16, packed 2x2: 1 x 8 B load */
+  LOLA_STORE_TEX32 = 6, /* FP32 texture: one 4-texel gather (tld4) per update */
+  LOLA_STORE_TEX16 = 7  /* FP16 texture: one 4-texel gather, widened by the texture unit */
 };
 
 enum {
@@ -113,7 +115,7 @@ typedef struct {
 /* Defaults: FP32 storage, plain accumulation, batch 16, 8 voxels per thread,
  * 8 rows per block, syncEachCall 1, exitOnError 1, no stats, device 0.
  * Environment overrides read by lolaCudaDefaultConfig: LOLACUDA_STORAGE
- * (f32|f16|bf16|f32q|f16q|bf16q), LOLACUDA_ACCUM (plain|kahan),
+ * (f32|f16|bf16|f32q|f16q|bf16q|tex32|tex16), LOLACUDA_ACCUM (plain|kahan),
  * LOLACUDA_BATCH, LOLACUDA_VPT, LOLACUDA_ROWS, LOLACUDA_SYNC, LOLACUDA_EXIT. */
 void lolaCudaDefaultConfig(LolaCudaConfig *config);
 

@@ -69,7 +69,8 @@ class LolaCudaStats(C.Structure):
                 ("tilePassesSkipped", C.c_int64)]
 
 
-STORAGE = {"f32": 0, "f16": 1, "bf16": 2, "f32q": 3, "f16q": 4, "bf16q": 5}
+STORAGE = {"f32": 0, "f16": 1, "bf16": 2, "f32q": 3, "f16q": 4, "bf16q": 5, "tex32": 6,
+           "tex16": 7}
 ACCUM = {"plain": 0, "kahan": 1}
 MAX_BATCH = 32
 

@@ -25,6 +25,7 @@ INCLUDE = REPO / "include"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_SOURCES = [
     "bp_f32.cu", "bp_f16.cu", "bp_bf16.cu", "bp_f32q.cu", "bp_f16q.cu", "bp_bf16q.cu",
+    "bp_tex32.cu", "bp_tex16.cu",
     "lolacuda_dispatch.cu", "lolacuda_probe.cu", "lolacuda_noalloc.cu",
 ]
 C_SOURCES = ["lolacuda_host.c"]
@@ -73,12 +74,15 @@ def build_lolacuda(force: bool = False, jobs: int | None = None) -> Path:
     headers = [CSRC / "bp_kernels.cuh", CSRC / "lolacuda_internal.h", INCLUDE / "lolaCuda.h"]
     common_inc = ["-I" + str(INCLUDE), "-I" + str(CSRC)]
 
+    # extra nvcc flags for tuning builds, e.g. LOLACUDA_NVCC_FLAGS=-DLOLA_MIN_BLOCKS=5
+    extra = os.environ.get("LOLACUDA_NVCC_FLAGS", "").split()
+
     def compile_cu(name: str) -> Path:
         src = CSRC / name
         obj = OBJ / (name + ".o")
         if force or _stale(obj, [src] + headers):
             _run([nvcc, *ARCH, "-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC",
-                  *common_inc, "-c", str(src), "-o", str(obj)])
+                  *extra, *common_inc, "-c", str(src), "-o", str(obj)])
         return obj
 
     def compile_c(name: str) -> Path:

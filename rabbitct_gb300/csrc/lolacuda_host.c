@@ -71,8 +71,9 @@ int lolaSetError(const char *fmt, ...)
 
 static int storageFromName(const char *s)
 {
-  static const char *names[] = { "f32", "f16", "bf16", "f32q", "f16q", "bf16q" };
-  for (int i = 0; i < 6; i++) {
+  static const char *names[] = { "f32", "f16", "bf16", "f32q", "f16q", "bf16q", "tex32",
+    "tex16" };
+  for (int i = 0; i < 8; i++) {
     const char *a = names[i], *b = s;
     while (*a && *b && tolower((unsigned char)*b) == *a) {
       a++;
@@ -119,7 +120,7 @@ void lolaCudaDefaultConfig(LolaCudaConfig *c)
 
 static int validateConfig(const LolaCudaConfig *c)
 {
-  if (c->storage < LOLA_STORE_F32 || c->storage > LOLA_STORE_BF16Q)
+  if (c->storage < LOLA_STORE_F32 || c->storage > LOLA_STORE_TEX16)
     return setError("invalid storage %d", c->storage);
   if (c->accumulation != LOLA_ACCUM_PLAIN && c->accumulation != LOLA_ACCUM_KAHAN)
     return setError("invalid accumulation %d", c->accumulation);
@@ -194,8 +195,15 @@ static int elemBytesOf(int storage)
   case LOLA_STORE_F32Q: return 16;
   case LOLA_STORE_F16Q: return 8;
   case LOLA_STORE_BF16Q: return 8;
+  case LOLA_STORE_TEX32: return 4;
+  case LOLA_STORE_TEX16: return 2;
   default: return 0;
   }
+}
+
+static int isTexture(int storage)
+{
+  return storage == LOLA_STORE_TEX32 || storage == LOLA_STORE_TEX16;
 }
 
 static int planRelease(LolaCudaPlan *p)
@@ -212,6 +220,9 @@ static int planRelease(LolaCudaPlan *p)
     cudaEventDestroy(p->events[i].stop);
   }
   free(p->events);
+  for (int i = 0; i < LOLA_MAX_BATCH; i++)
+    if (p->store.texObjects[i])
+      cudaDestroyTextureObject((cudaTextureObject_t)p->store.texObjects[i]);
   cudaFree(p->d_volume);
   cudaFree(p->d_ring);
   cudaFree(p->d_stage);
@@ -254,14 +265,16 @@ static int planInit(LolaCudaPlan *p)
   s->margin = LOLA_MARGIN;
   s->width = g->imageWidth;
   s->height = g->imageHeight;
-  s->pitch = g->imageWidth + 2 * LOLA_MARGIN;
+  /* pitch a multiple of 32 pixels: row starts stay 64 B aligned for every
+     element size, which texture fetches from pitched memory require */
+  s->pitch = (g->imageWidth + 2 * LOLA_MARGIN + 31) & ~31;
   s->rows = g->imageHeight + 2 * LOLA_MARGIN;
   /* index arithmetic in the kernel is exact below 2^23 pixels */
   if ((long long)s->pitch * s->rows >= (1LL << 23) - 2 * (long long)s->pitch)
     return setError("detector %dx%d too large (padded image must stay below 2^23 pixels)",
         g->imageWidth, g->imageHeight);
   const size_t px = (size_t)s->pitch * (size_t)s->rows;
-  s->slotElems = (px + 63) & ~(size_t)63;
+  s->slotElems = (px + 255) & ~(size_t)255;  /* slot bases 512 B aligned */
   p->imageElems = (size_t)g->imageWidth * (size_t)g->imageHeight;
 
   const size_t nvox = (size_t)g->problemSize * g->problemSize * g->problemSize;
@@ -270,6 +283,29 @@ static int planInit(LolaCudaPlan *p)
   CUDA_TRY(cudaMalloc(&p->d_ring, (size_t)p->cfg.batch * s->slotElems * s->elemBytes));
   CUDA_TRY(cudaMemsetAsync(p->d_ring, 0, (size_t)p->cfg.batch * s->slotElems * s->elemBytes,
       p->stream));
+  if (isTexture(s->storage)) {
+    for (int i = 0; i < p->cfg.batch; i++) {
+      struct cudaResourceDesc rd;
+      memset(&rd, 0, sizeof(rd));
+      rd.resType = cudaResourceTypePitch2D;
+      rd.res.pitch2D.devPtr = (char *)p->d_ring + (size_t)i * s->slotElems * s->elemBytes;
+      rd.res.pitch2D.desc = cudaCreateChannelDesc(8 * s->elemBytes, 0, 0, 0,
+          cudaChannelFormatKindFloat);
+      rd.res.pitch2D.width = (size_t)s->pitch;
+      rd.res.pitch2D.height = (size_t)s->rows;
+      rd.res.pitch2D.pitchInBytes = (size_t)s->pitch * s->elemBytes;
+      struct cudaTextureDesc td;
+      memset(&td, 0, sizeof(td));
+      td.addressMode[0] = cudaAddressModeBorder;
+      td.addressMode[1] = cudaAddressModeBorder;
+      td.filterMode = cudaFilterModePoint;
+      td.readMode = cudaReadModeElementType;
+      td.normalizedCoords = 0;
+      cudaTextureObject_t t = 0;
+      CUDA_TRY(cudaCreateTextureObject(&t, &rd, &td, NULL));
+      s->texObjects[i] = (unsigned long long)t;
+    }
+  }
   CUDA_TRY(cudaMalloc((void **)&p->d_stage, (size_t)p->cfg.batch * p->imageElems * sizeof(float)));
   CUDA_TRY(cudaMalloc((void **)&p->d_counters, 3 * sizeof(unsigned long long)));
   CUDA_TRY(cudaMemsetAsync(p->d_counters, 0, 3 * sizeof(unsigned long long), p->stream));
@@ -604,13 +640,14 @@ int lolaCudaDeviceSynchronize(void)
 
 static LolaCudaPlan *gPlan = NULL;
 static uint32_t gTotalProjections = 0; /* known with -a (src/rabbitRunner.c:209-210) */
-static int gExitOnError = 1;
 
 static int moduleFail(const char *where)
 {
+  LolaCudaConfig c;
+  lolaCudaGetConfig(&c);
   fprintf(stderr, "LolaCUDA %s: %s\n", where, gLastError);
   fflush(stderr);
-  if (gExitOnError)
+  if (c.exitOnError)
     exit(EXIT_FAILURE);
   return 0;
 }
@@ -619,7 +656,6 @@ int lolaCudaPrepare(RabbitCtGlobalData *d)
 {
   LolaCudaConfig c;
   lolaCudaGetConfig(&c);
-  gExitOnError = c.exitOnError;
   if (d == NULL) {
     setError("null global data");
     return moduleFail("prepare");

@@ -29,6 +29,8 @@ typedef struct {
   int32_t height;       /* detector height */
   int32_t reserved;
   size_t slotElems;     /* pixels per ring slot (>= pitch * rows, 256 B multiple) */
+  /* texture layouts: one texture object per ring slot (cudaTextureObject_t) */
+  unsigned long long texObjects[LOLA_MAX_BATCH];
 } LolaStoreDesc;
 
 /* One projection of a kernel pass: the FP64 matrix and its FP32 voxel steps. */
@@ -51,7 +53,7 @@ typedef struct {
   LolaPassProj proj[LOLA_MAX_BATCH];
 } LolaPassParams;
 
-/* Kernel launchers (lolacuda_kernels.cu).  Return 0 on success or a
+/* Kernel launchers (lolacuda_dispatch.cu).  Return 0 on success or a
  * cudaError_t value. */
 int lolaLaunchPack(const LolaStoreDesc *store, const float *d_src, size_t srcStride,
     void *d_ring, int slot0, int count, void *stream);

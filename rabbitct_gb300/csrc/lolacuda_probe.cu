@@ -42,10 +42,11 @@ __global__ void __launch_bounds__(256) issueProbe(float *out, int iters, float a
     out[blockIdx.x * blockDim.x + threadIdx.x] = s;
 }
 
-/* kind: 0 = 4 x FP32 taps, 1 = 4 x 16-bit taps, 2 = 1 x 16 B quad, 3 = 1 x 8 B quad */
+/* kind: 0 = 4 x FP32 taps, 1 = 4 x 16-bit taps, 2 = 1 x 16 B quad, 3 = 1 x 8 B quad,
+ * 4 = one 4-texel texture gather (tld4) */
 template <int KIND>
 __global__ void __launch_bounds__(256) gatherProbe(const void *img, int pitch, int rows,
-    int iters, float *out)
+    int iters, float *out, cudaTextureObject_t tex)
 {
   const int lane = threadIdx.x & 31;
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -67,9 +68,14 @@ __global__ void __launch_bounds__(256) gatherProbe(const void *img, int pitch, i
     } else if (KIND == 2) {
       const float4 q = __ldg(static_cast<const float4 *>(img) + idx);
       acc += (q.x + q.y) + (q.z + q.w);
-    } else {
+    } else if (KIND == 3) {
       const uint2 q = __ldg(static_cast<const uint2 *>(img) + idx);
       acc += __uint_as_float(q.x) + __uint_as_float(q.y);
+    } else {
+      const float cx = (float)(idx % (uint32_t)pitch) + 1.0f;
+      const float cy = (float)(idx / (uint32_t)pitch) + 1.0f;
+      const float4 g = tex2Dgather<float4>(tex, cx, cy, 0);
+      acc += (g.x + g.y) + (g.z + g.w);
     }
   }
   if (acc == 1234.5f)
@@ -117,7 +123,7 @@ extern "C" double lolaCudaProbeIssueRate(void)
  * (LOLA_STORE_*) over a width x height detector padded like the pass kernel. */
 extern "C" double lolaCudaProbeGatherRate(int storage, int width, int height)
 {
-  const int pitch = width + 128, rows = height + 128;
+  const int pitch = (width + 128 + 31) & ~31, rows = height + 128;
   int kind, elem;
   switch (storage) {
   case LOLA_STORE_F32: kind = 0; elem = 4; break;
@@ -126,6 +132,8 @@ extern "C" double lolaCudaProbeGatherRate(int storage, int width, int height)
   case LOLA_STORE_F32Q: kind = 2; elem = 16; break;
   case LOLA_STORE_F16Q:
   case LOLA_STORE_BF16Q: kind = 3; elem = 8; break;
+  case LOLA_STORE_TEX32: kind = 4; elem = 4; break;
+  case LOLA_STORE_TEX16: kind = 4; elem = 2; break;
   default: return -1.0;
   }
   const size_t bytes = (size_t)pitch * rows * elem;
@@ -138,6 +146,25 @@ extern "C" double lolaCudaProbeGatherRate(int storage, int width, int height)
     return -1.0;
   }
   cudaMemset(img, 0, bytes);
+  cudaTextureObject_t tex = 0;
+  if (kind == 4) {
+    cudaResourceDesc rd = {};
+    rd.resType = cudaResourceTypePitch2D;
+    rd.res.pitch2D.devPtr = img;
+    rd.res.pitch2D.desc = cudaCreateChannelDesc(8 * elem, 0, 0, 0, cudaChannelFormatKindFloat);
+    rd.res.pitch2D.width = (size_t)pitch;
+    rd.res.pitch2D.height = (size_t)rows;
+    rd.res.pitch2D.pitchInBytes = (size_t)pitch * elem;
+    cudaTextureDesc td = {};
+    td.addressMode[0] = td.addressMode[1] = cudaAddressModeBorder;
+    td.filterMode = cudaFilterModePoint;
+    td.readMode = cudaReadModeElementType;
+    if (cudaCreateTextureObject(&tex, &rd, &td, nullptr) != cudaSuccess) {
+      cudaFree(img);
+      cudaFree(out);
+      return -1.0;
+    }
+  }
   const int sms = smCount();
   const int blocks = sms * 8, threads = 256, iters = 2048;
   cudaEvent_t e0, e1;
@@ -145,10 +172,11 @@ extern "C" double lolaCudaProbeGatherRate(int storage, int width, int height)
   cudaEventCreate(&e1);
   auto launch = [&](int it) {
     switch (kind) {
-    case 0: gatherProbe<0><<<blocks, threads>>>(img, pitch, rows, it, out); break;
-    case 1: gatherProbe<1><<<blocks, threads>>>(img, pitch, rows, it, out); break;
-    case 2: gatherProbe<2><<<blocks, threads>>>(img, pitch, rows, it, out); break;
-    default: gatherProbe<3><<<blocks, threads>>>(img, pitch, rows, it, out); break;
+    case 0: gatherProbe<0><<<blocks, threads>>>(img, pitch, rows, it, out, tex); break;
+    case 1: gatherProbe<1><<<blocks, threads>>>(img, pitch, rows, it, out, tex); break;
+    case 2: gatherProbe<2><<<blocks, threads>>>(img, pitch, rows, it, out, tex); break;
+    case 3: gatherProbe<3><<<blocks, threads>>>(img, pitch, rows, it, out, tex); break;
+    default: gatherProbe<4><<<blocks, threads>>>(img, pitch, rows, it, out, tex); break;
     }
   };
   launch(64);
@@ -160,6 +188,8 @@ extern "C" double lolaCudaProbeGatherRate(int storage, int width, int height)
   cudaEventElapsedTime(&ms, e0, e1);
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
+  if (tex)
+    cudaDestroyTextureObject(tex);
   cudaFree(img);
   cudaFree(out);
   if (cudaGetLastError() != cudaSuccess || ms <= 0.0f)

@@ -1,9 +1,10 @@
 """Parity of the CUDA path (through the C ABI) with the FP64 LolaBunny oracle.
 
 Bars (the FP64 oracle is the reference of every comparison):
-  FP32 storage, plain or Kahan       relative RMSE <= 1e-5 (and <= 1e-5 vs the
+  FP32 storage (plain, quad or texture), plain or Kahan accumulation
+                                     relative RMSE <= 1e-5 (and <= 1e-5 vs the
                                      FP32-accumulating LolaBunny restatement)
-  FP16 storage (plain or quad)       relative RMSE <= 1e-3
+  FP16 storage (plain, quad or texture) relative RMSE <= 1e-3
   BF16 storage (plain or quad)       relative RMSE <= 4e-3 (8-bit mantissa)
 """
 from __future__ import annotations
@@ -17,7 +18,8 @@ from rabbitct_gb300 import metrics, synth
 
 pytestmark = pytest.mark.gpu
 
-BAR = {"f32": 1e-5, "f32q": 1e-5, "f16": 1e-3, "f16q": 1e-3, "bf16": 4e-3, "bf16q": 4e-3}
+BAR = {"f32": 1e-5, "f32q": 1e-5, "f16": 1e-3, "f16q": 1e-3, "bf16": 4e-3, "bf16q": 4e-3,
+       "tex32": 1e-5, "tex16": 1e-3}
 
 
 @pytest.fixture(scope="module")
@@ -52,7 +54,8 @@ def scan12():
     return _scan()
 
 
-@pytest.mark.parametrize("storage", ["f32", "f32q", "f16", "f16q", "bf16", "bf16q"])
+@pytest.mark.parametrize("storage", ["f32", "f32q", "f16", "f16q", "bf16", "bf16q", "tex32",
+                                     "tex16"])
 @pytest.mark.parametrize("accum", ["plain", "kahan"])
 def test_storage_accum_vs_oracle(lib, scan12, storage, accum):
     from rabbitct_gb300.lolacuda import Plan
