@@ -50,9 +50,9 @@ METRIC = "GUPS (1e9 voxel updates/s) N=512,1024: FP16-stored vs FP32 path, RMSE 
 # replace the index, address and widening work by 2 coordinate adds and one
 # 4-texel gather.
 INSTR_PER_UPDATE = {"f32": 25, "f16": 29, "bf16": 29, "f32q": 22, "f16q": 26, "bf16q": 26,
-                    "tex32": 21, "tex16": 21}
+                    "tex32": 21, "tex16": 21, "f16qx": 24, "f32qx": 22}
 STORAGE_IDS = {"f32": 0, "f16": 1, "bf16": 2, "f32q": 3, "f16q": 4, "bf16q": 5, "tex32": 6,
-               "tex16": 7}
+               "tex16": 7, "f16qx": 8, "f32qx": 9}
 
 
 def parse_args():
@@ -309,7 +309,7 @@ def roofline(args, lib, storage, st, probes) -> dict:
     # HBM view: volume read + write once per pass plus the stored projections
     # read once per pass from L2 misses at most (algorithmic floor).
     elem = {"f32": 4, "f16": 2, "bf16": 2, "f32q": 16, "f16q": 8, "bf16q": 8, "tex32": 4,
-            "tex16": 2}[storage]
+            "tex16": 2, "f16qx": 8, "f32qx": 16}[storage]
     vol_bytes = 8.0 * args.n ** 3
     proj_bytes = args.batch * (args.width + 128) * (args.height + 128) * elem
     hbm_gbs = (vol_bytes + proj_bytes) / (avg_ms * 1e-3) / 1e9

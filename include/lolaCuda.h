@@ -91,7 +91,10 @@ enum {
   LOLA_STORE_F16Q = 4,  /* FP16, packed 2x2: 1 x 8 B load */
   LOLA_STORE_BF16Q = 5, /* BF16, packed 2x2: 1 x 8 B load */
   LOLA_STORE_TEX32 = 6, /* FP32 texture: one 4-texel gather (tld4) per update */
-  LOLA_STORE_TEX16 = 7  /* FP16 texture: one 4-texel gather, widened by the texture unit */
+  LOLA_STORE_TEX16 = 7, /* FP16 texture: one 4-texel gather, widened by the texture unit */
+  LOLA_STORE_F16QX = 8, /* FP16 2x2 quads read both by loads and as an RGBA16F texture:
+                           each thread's voxels alternate between the two paths */
+  LOLA_STORE_F32QX = 9  /* FP32 2x2 quads, loads + RGBA32F texture */
 };
 
 enum {
@@ -115,7 +118,7 @@ typedef struct {
 /* Defaults: FP32 storage, plain accumulation, batch 16, 8 voxels per thread,
  * 8 rows per block, syncEachCall 1, exitOnError 1, no stats, device 0.
  * Environment overrides read by lolaCudaDefaultConfig: LOLACUDA_STORAGE
- * (f32|f16|bf16|f32q|f16q|bf16q|tex32|tex16), LOLACUDA_ACCUM (plain|kahan),
+ * (f32|f16|bf16|f32q|f16q|bf16q|tex32|tex16|f16qx|f32qx), LOLACUDA_ACCUM (plain|kahan),
  * LOLACUDA_BATCH, LOLACUDA_VPT, LOLACUDA_ROWS, LOLACUDA_SYNC, LOLACUDA_EXIT. */
 void lolaCudaDefaultConfig(LolaCudaConfig *config);
 

@@ -52,6 +52,11 @@ struct TileProj {
   float su[3], sv[3], sw[3]; /* per-axis steps (x, y, z) of u', v', w */
   int mode;
   int slot;
+  float fx0, fx1, fy0, fy1;  /* footprint of the tile on the detector (pixels) */
+  /* shared-memory staging (staged pass only) */
+  int seq;                   /* index among the staged projections of the pass */
+  int bx, by;                /* box origin in the padded image */
+  float sbias;               /* 2^23 + box-local index of detector pixel (0, 0) */
 };
 
 __device__ __forceinline__ float rcpApprox(float x)
@@ -70,6 +75,7 @@ template <int S> struct Layout;
 
 template <> struct Layout<LOLA_STORE_F32> {
   static constexpr bool kTex = false;
+  static constexpr bool kMixed = false;
   typedef float Elem;
   static constexpr bool kQuad = false;
   __device__ static __forceinline__ void fetch(const void *img, uint32_t idx, int pitch,
@@ -89,6 +95,7 @@ template <> struct Layout<LOLA_STORE_F32> {
 
 template <> struct Layout<LOLA_STORE_F16> {
   static constexpr bool kTex = false;
+  static constexpr bool kMixed = false;
   typedef __half Elem;
   static constexpr bool kQuad = false;
   __device__ static __forceinline__ void fetch(const void *img, uint32_t idx, int pitch,
@@ -108,6 +115,7 @@ template <> struct Layout<LOLA_STORE_F16> {
 
 template <> struct Layout<LOLA_STORE_BF16> {
   static constexpr bool kTex = false;
+  static constexpr bool kMixed = false;
   typedef __nv_bfloat16 Elem;
   static constexpr bool kQuad = false;
   __device__ static __forceinline__ void fetch(const void *img, uint32_t idx, int pitch,
@@ -127,6 +135,7 @@ template <> struct Layout<LOLA_STORE_BF16> {
 
 template <> struct Layout<LOLA_STORE_F32Q> {
   static constexpr bool kTex = false;
+  static constexpr bool kMixed = false;
   typedef float4 Elem;
   static constexpr bool kQuad = true;
   __device__ static __forceinline__ void fetch(const void *img, uint32_t idx, int,
@@ -147,6 +156,7 @@ template <> struct Layout<LOLA_STORE_F32Q> {
 
 template <> struct Layout<LOLA_STORE_F16Q> {
   static constexpr bool kTex = false;
+  static constexpr bool kMixed = false;
   typedef uint2 Elem;
   static constexpr bool kQuad = true;
   __device__ static __forceinline__ void fetch(const void *img, uint32_t idx, int,
@@ -177,6 +187,7 @@ template <> struct Layout<LOLA_STORE_F16Q> {
 
 template <> struct Layout<LOLA_STORE_BF16Q> {
   static constexpr bool kTex = false;
+  static constexpr bool kMixed = false;
   typedef uint2 Elem;
   static constexpr bool kQuad = true;
   __device__ static __forceinline__ void fetch(const void *img, uint32_t idx, int,
@@ -208,6 +219,7 @@ template <> struct Layout<LOLA_STORE_BF16Q> {
  * (i, j+1), (i+1, j+1), (i+1, j), (i, j). */
 template <> struct Layout<LOLA_STORE_TEX32> {
   static constexpr bool kTex = true;
+  static constexpr bool kMixed = false;
   typedef float Elem;
   static constexpr bool kQuad = false;
   __device__ static __forceinline__ void store(void *dst, size_t o, float a, float, float, float)
@@ -218,6 +230,7 @@ template <> struct Layout<LOLA_STORE_TEX32> {
 
 template <> struct Layout<LOLA_STORE_TEX16> {
   static constexpr bool kTex = true;
+  static constexpr bool kMixed = false;
   typedef __half Elem;
   static constexpr bool kQuad = false;
   __device__ static __forceinline__ void store(void *dst, size_t o, float a, float, float, float)
@@ -234,6 +247,35 @@ __device__ __forceinline__ void texTaps(unsigned long long tex, float cx, float 
   p10 = g.z;
   p01 = g.x;
   p11 = g.y;
+}
+
+
+/* Mixed layouts: the 2x2 quads of the F16Q / F32Q layouts, also bound as an
+ * RGBA texture (one texel = one quad).  Voxels whose bit is set in
+ * LOLA_MIXED_TEX_MASK (default: 2 of every 8, the best split measured on
+ * GB300) fetch their quad through the texture unit (a point fetch, widened
+ * to FP32 there), the others through the load path, so both gather pipes
+ * work in parallel. */
+#ifndef LOLA_MIXED_TEX_MASK
+#define LOLA_MIXED_TEX_MASK 0x8888u
+#endif
+
+template <> struct Layout<LOLA_STORE_F16QX> : Layout<LOLA_STORE_F16Q> {
+  static constexpr bool kMixed = true;
+};
+
+template <> struct Layout<LOLA_STORE_F32QX> : Layout<LOLA_STORE_F32Q> {
+  static constexpr bool kMixed = true;
+};
+
+__device__ __forceinline__ void texQuad(unsigned long long tex, float cx, float cy, float &p00,
+    float &p10, float &p01, float &p11)
+{
+  const float4 q = tex2D<float4>((cudaTextureObject_t)tex, cx, cy);
+  p00 = q.x;
+  p10 = q.y;
+  p01 = q.z;
+  p11 = q.w;
 }
 
 /* ---- packing: FP32 detector image -> zero-padded stored layout ------------- */
@@ -321,6 +363,10 @@ __device__ __forceinline__ void applyProjection(const TileProj &tp, const void *
          texture; gathering at that + 1 selects it as the lower-left tap */
       const float off = (float)a.margin + 1.0f;
       texTaps(tex, tx + off, ty + off, p00, p10, p01, p11);
+    } else if (Layout<S>::kMixed && ((LOLA_MIXED_TEX_MASK >> k) & 1u)) {
+      /* point fetch of texel (tx + M, ty + M): any coordinate inside it works */
+      const float off = (float)a.margin + 0.5f;
+      texQuad(tex, tx + off, ty + off, p00, p10, p01, p11);
     } else {
       uint32_t idx = __float_as_uint(fmaf(ty, pitchF, tx + biasF)) - 0x4B000000u;
       idx = min(idx, maxIdx);  /* memory-safety net; never active on valid input */
@@ -343,32 +389,16 @@ __device__ __forceinline__ void applyProjection(const TileProj &tp, const void *
   }
 }
 
-/* Resident blocks per SM requested from the register allocator.  The pass is
- * bound by the latency of its gathers, so occupancy pays: 48 warps per SM
- * (40 registers for 8 voxels x 8 rows) measured 25 % faster on GB300 than the
- * compiler's own choice of 61 registers and 32 warps.  LOLA_MIN_BLOCKS
- * overrides it at build time (0 = the compiler's choice). */
-template <int VPT, int ROWS> struct MinBlocks {
-  /* 8 voxels per thread: 48 warps per SM (40 registers); 16 voxels: 20-24
-     warps, which keeps their accumulators out of local memory */
-  static constexpr int kValue = (VPT <= 8) ? 1536 / (32 * ROWS) : 640 / (32 * ROWS);
-};
-#ifdef LOLA_MIN_BLOCKS
-#define LOLA_PASS_MIN_BLOCKS(VPT, ROWS) LOLA_MIN_BLOCKS
-#else
-#define LOLA_PASS_MIN_BLOCKS(VPT, ROWS) (MinBlocks<VPT, ROWS>::kValue)
-#endif
-
-template <int S, int VPT, int ROWS, bool KAHAN>
-__global__ void __launch_bounds__(32 * ROWS, LOLA_PASS_MIN_BLOCKS(VPT, ROWS))
-    passKernel(const PassArgs a, const LolaPassParams P)
+/* Per-(tile, projection) setup shared by the pass kernels: the FP64 tile
+ * origin (phase A, one thread per projection) and the footprint and mode from
+ * the 8 tile corners (phase B, 8 lanes per projection).  Ends with the block
+ * synchronised and sp[0 .. count) complete.  nthreads is a multiple of 32. */
+template <int ROWS, int VPT>
+__device__ __forceinline__ void setupTile(const LolaPassParams &P, const PassArgs &a,
+    TileProj *sp, int tid, int nthreads, int x0, int y0, int z0)
 {
-  __shared__ TileProj sp[LOLA_MAX_BATCH];
   const int N = P.N;
-  const int x0 = blockIdx.x * 32, y0 = blockIdx.y * ROWS, z0 = blockIdx.z * VPT;
-  const int tid = threadIdx.y * 32 + threadIdx.x;
   const int count = P.count;
-
   /* -- setup A: FP64 projection of the tile origin, one thread per view -- */
   if (tid < count) {
     const LolaPassProj &pp = P.proj[tid];
@@ -400,7 +430,7 @@ __global__ void __launch_bounds__(32 * ROWS, LOLA_PASS_MIN_BLOCKS(VPT, ROWS))
 
   /* -- setup B: footprint of the tile from its 8 corners, 8 lanes per view -- */
   const int ex = min(32, N - x0) - 1, ey = min(ROWS, N - y0) - 1, ez = min(VPT, N - z0) - 1;
-  for (int base = 0; base < 8 * count; base += 32 * ROWS) {
+  for (int base = 0; base < 8 * count; base += nthreads) {
     const int t = base + tid;
     const bool active = t < 8 * count;
     const int p = active ? (t >> 3) : 0;
@@ -438,9 +468,43 @@ __global__ void __launch_bounds__(32 * ROWS, LOLA_PASS_MIN_BLOCKS(VPT, ROWS))
       else
         mode = MODE_SLOW;
       sp[p].mode = mode;
+      sp[p].fx0 = mnx - slack;
+      sp[p].fx1 = mxx + slack;
+      sp[p].fy0 = mny - slack;
+      sp[p].fy1 = mxy + slack;
     }
   }
   __syncthreads();
+
+}
+
+/* Resident blocks per SM requested from the register allocator.  The pass is
+ * bound by the latency of its gathers, so occupancy pays: 48 warps per SM
+ * (40 registers for 8 voxels x 8 rows) measured 25 % faster on GB300 than the
+ * compiler's own choice of 61 registers and 32 warps.  LOLA_MIN_BLOCKS
+ * overrides it at build time (0 = the compiler's choice). */
+template <int VPT, int ROWS> struct MinBlocks {
+  /* 8 voxels per thread: 48 warps per SM (40 registers); 16 voxels: 20-24
+     warps, which keeps their accumulators out of local memory */
+  static constexpr int kValue = (VPT <= 8) ? 1536 / (32 * ROWS) : 640 / (32 * ROWS);
+};
+#ifdef LOLA_MIN_BLOCKS
+#define LOLA_PASS_MIN_BLOCKS(VPT, ROWS) LOLA_MIN_BLOCKS
+#else
+#define LOLA_PASS_MIN_BLOCKS(VPT, ROWS) (MinBlocks<VPT, ROWS>::kValue)
+#endif
+
+template <int S, int VPT, int ROWS, bool KAHAN>
+__global__ void __launch_bounds__(32 * ROWS, LOLA_PASS_MIN_BLOCKS(VPT, ROWS))
+    passKernel(const PassArgs a, const LolaPassParams P)
+{
+  __shared__ TileProj sp[LOLA_MAX_BATCH];
+  const int N = P.N;
+  const int x0 = blockIdx.x * 32, y0 = blockIdx.y * ROWS, z0 = blockIdx.z * VPT;
+  const int tid = threadIdx.y * 32 + threadIdx.x;
+  const int count = P.count;
+
+  setupTile<ROWS, VPT>(P, a, sp, tid, 32 * ROWS, x0, y0, z0);
 
   if (a.tileCounters != nullptr && tid == 0) {
     unsigned long long nSkip = 0, nFast = 0, nSlow = 0;
@@ -473,7 +537,8 @@ __global__ void __launch_bounds__(32 * ROWS, LOLA_PASS_MIN_BLOCKS(VPT, ROWS))
       continue;
     const TileProj tp = sp[p];
     const void *img = static_cast<const char *>(a.ring) + (size_t)tp.slot * a.slotBytes;
-    const unsigned long long tex = Layout<S>::kTex ? a.tex[tp.slot] : 0ull;
+    const unsigned long long tex =
+        (Layout<S>::kTex || Layout<S>::kMixed) ? a.tex[tp.slot] : 0ull;
     if (mode == MODE_FAST)
       applyProjection<S, VPT, KAHAN, false>(tp, img, tex, a, fi, fj, acc, comp);
     else

@@ -17,6 +17,8 @@ LOLA_DECLARE(F16Q)
 LOLA_DECLARE(BF16Q)
 LOLA_DECLARE(TEX32)
 LOLA_DECLARE(TEX16)
+LOLA_DECLARE(F16QX)
+LOLA_DECLARE(F32QX)
 
 static_assert(sizeof(LolaPassParams) < 32000, "pass parameters exceed the kernel parameter limit");
 
@@ -34,6 +36,8 @@ extern "C" int lolaLaunchPack(const LolaStoreDesc *st, const float *d_src, size_
   case LOLA_STORE_BF16Q: return lolaLaunchPack_BF16Q(st, d_src, srcStride, d_ring, slot0, count, stream);
   case LOLA_STORE_TEX32: return lolaLaunchPack_TEX32(st, d_src, srcStride, d_ring, slot0, count, stream);
   case LOLA_STORE_TEX16: return lolaLaunchPack_TEX16(st, d_src, srcStride, d_ring, slot0, count, stream);
+  case LOLA_STORE_F16QX: return lolaLaunchPack_F16QX(st, d_src, srcStride, d_ring, slot0, count, stream);
+  case LOLA_STORE_F32QX: return lolaLaunchPack_F32QX(st, d_src, srcStride, d_ring, slot0, count, stream);
   default: return (int)cudaErrorInvalidValue;
   }
 }
@@ -54,6 +58,8 @@ extern "C" int lolaLaunchBackproject(const LolaStoreDesc *st, const LolaPassPara
   case LOLA_STORE_BF16Q: return lolaLaunchPass_BF16Q(st, P, d_ring, d_volume, d_tileCounters, stream);
   case LOLA_STORE_TEX32: return lolaLaunchPass_TEX32(st, P, d_ring, d_volume, d_tileCounters, stream);
   case LOLA_STORE_TEX16: return lolaLaunchPass_TEX16(st, P, d_ring, d_volume, d_tileCounters, stream);
+  case LOLA_STORE_F16QX: return lolaLaunchPass_F16QX(st, P, d_ring, d_volume, d_tileCounters, stream);
+  case LOLA_STORE_F32QX: return lolaLaunchPass_F32QX(st, P, d_ring, d_volume, d_tileCounters, stream);
   default: return (int)cudaErrorInvalidValue;
   }
 }

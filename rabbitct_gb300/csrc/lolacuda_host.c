@@ -72,8 +72,8 @@ int lolaSetError(const char *fmt, ...)
 static int storageFromName(const char *s)
 {
   static const char *names[] = { "f32", "f16", "bf16", "f32q", "f16q", "bf16q", "tex32",
-    "tex16" };
-  for (int i = 0; i < 8; i++) {
+    "tex16", "f16qx", "f32qx" };
+  for (int i = 0; i < 10; i++) {
     const char *a = names[i], *b = s;
     while (*a && *b && tolower((unsigned char)*b) == *a) {
       a++;
@@ -120,7 +120,7 @@ void lolaCudaDefaultConfig(LolaCudaConfig *c)
 
 static int validateConfig(const LolaCudaConfig *c)
 {
-  if (c->storage < LOLA_STORE_F32 || c->storage > LOLA_STORE_TEX16)
+  if (c->storage < LOLA_STORE_F32 || c->storage > LOLA_STORE_F32QX)
     return setError("invalid storage %d", c->storage);
   if (c->accumulation != LOLA_ACCUM_PLAIN && c->accumulation != LOLA_ACCUM_KAHAN)
     return setError("invalid accumulation %d", c->accumulation);
@@ -197,13 +197,24 @@ static int elemBytesOf(int storage)
   case LOLA_STORE_BF16Q: return 8;
   case LOLA_STORE_TEX32: return 4;
   case LOLA_STORE_TEX16: return 2;
+  case LOLA_STORE_F16QX: return 8;
+  case LOLA_STORE_F32QX: return 16;
   default: return 0;
   }
 }
 
+/* Layouts read (also) through the texture unit, and their texel format:
+ * 1 channel for the gather layouts, 4 (one 2x2 quad per texel) for the
+ * mixed ones. */
 static int isTexture(int storage)
 {
-  return storage == LOLA_STORE_TEX32 || storage == LOLA_STORE_TEX16;
+  return storage == LOLA_STORE_TEX32 || storage == LOLA_STORE_TEX16 ||
+         storage == LOLA_STORE_F16QX || storage == LOLA_STORE_F32QX;
+}
+
+static int texChannels(int storage)
+{
+  return (storage == LOLA_STORE_F16QX || storage == LOLA_STORE_F32QX) ? 4 : 1;
 }
 
 static int planRelease(LolaCudaPlan *p)
@@ -289,8 +300,10 @@ static int planInit(LolaCudaPlan *p)
       memset(&rd, 0, sizeof(rd));
       rd.resType = cudaResourceTypePitch2D;
       rd.res.pitch2D.devPtr = (char *)p->d_ring + (size_t)i * s->slotElems * s->elemBytes;
-      rd.res.pitch2D.desc = cudaCreateChannelDesc(8 * s->elemBytes, 0, 0, 0,
-          cudaChannelFormatKindFloat);
+      const int ch = texChannels(s->storage);
+      const int bits = 8 * s->elemBytes / ch;
+      rd.res.pitch2D.desc = cudaCreateChannelDesc(bits, ch > 1 ? bits : 0, ch > 1 ? bits : 0,
+          ch > 1 ? bits : 0, cudaChannelFormatKindFloat);
       rd.res.pitch2D.width = (size_t)s->pitch;
       rd.res.pitch2D.height = (size_t)s->rows;
       rd.res.pitch2D.pitchInBytes = (size_t)s->pitch * s->elemBytes;

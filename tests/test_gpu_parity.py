@@ -19,7 +19,7 @@ from rabbitct_gb300 import metrics, synth
 pytestmark = pytest.mark.gpu
 
 BAR = {"f32": 1e-5, "f32q": 1e-5, "f16": 1e-3, "f16q": 1e-3, "bf16": 4e-3, "bf16q": 4e-3,
-       "tex32": 1e-5, "tex16": 1e-3}
+       "tex32": 1e-5, "tex16": 1e-3, "f16qx": 1e-3, "f32qx": 1e-5}
 
 
 @pytest.fixture(scope="module")
@@ -55,7 +55,7 @@ def scan12():
 
 
 @pytest.mark.parametrize("storage", ["f32", "f32q", "f16", "f16q", "bf16", "bf16q", "tex32",
-                                     "tex16"])
+                                     "tex16", "f16qx", "f32qx"])
 @pytest.mark.parametrize("accum", ["plain", "kahan"])
 def test_storage_accum_vs_oracle(lib, scan12, storage, accum):
     from rabbitct_gb300.lolacuda import Plan
