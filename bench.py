@@ -71,6 +71,8 @@ def parse_args():
     ap.add_argument("--batch", type=int, default=16)
     ap.add_argument("--vpt", type=int, default=8)
     ap.add_argument("--rows", type=int, default=8)
+    ap.add_argument("--staging", type=int, default=None,
+                    help="1/0: force shared-memory staging on/off (default: library default)")
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--cpu-views", type=int, default=8,
                     help="projections in the bounded CPU-baseline sample")
@@ -261,7 +263,8 @@ def time_device(args, dist, lib_mod, scan, vs, o, d_images, storage, clocks=None
     from rabbitct_gb300.lolacuda import Plan
     W, H = scan.width, scan.height
     with Plan(args.n, vs, o, W, H, storage=storage, batch=args.batch,
-              voxels_per_thread=args.vpt, rows_per_block=args.rows, collect_stats=1) as p:
+              voxels_per_thread=args.vpt, rows_per_block=args.rows, collect_stats=1,
+              staging=args.staging) as p:
         for _ in range(args.warmup):
             p.zero()
             p.backproject_device(d_images.ptr, W * H, scan.matrices)
@@ -348,7 +351,7 @@ def time_e2e(args, dist, scan, vs, o, storage) -> dict:
     mats = np.ascontiguousarray(scan.matrices)
     check(lib.lolaCudaSetConfig(config(storage=storage, batch=args.batch,
                                        voxels_per_thread=args.vpt, rows_per_block=args.rows,
-                                       exit_on_error=0)), "config")
+                                       exit_on_error=0, staging=args.staging)), "config")
     prepare, iterate, finish = module_functions(lib, "lolaCuda")
     times = []
     for step in range(1 + args.e2e_steps):

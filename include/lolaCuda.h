@@ -112,14 +112,20 @@ typedef struct {
   int32_t exitOnError;   /* module API: print + exit(EXIT_FAILURE) on error */
   int32_t collectStats;  /* record CUDA events around every backprojection pass */
   int32_t device;        /* CUDA device ordinal */
-  int32_t reserved[7];
+  int32_t staging;       /* 1: stage each tile's projection footprint in shared
+                            memory with tensor copies where it fits; 0: gather
+                            through the load / texture path (default: measured
+                            faster on GB300 at N=1024) */
+  int32_t reserved[6];
 } LolaCudaConfig;
 
 /* Defaults: FP32 storage, plain accumulation, batch 16, 8 voxels per thread,
- * 8 rows per block, syncEachCall 1, exitOnError 1, no stats, device 0.
+ * 8 rows per block, syncEachCall 1, exitOnError 1, no stats, device 0,
+ * staging 0.
  * Environment overrides read by lolaCudaDefaultConfig: LOLACUDA_STORAGE
  * (f32|f16|bf16|f32q|f16q|bf16q|tex32|tex16|f16qx|f32qx), LOLACUDA_ACCUM (plain|kahan),
- * LOLACUDA_BATCH, LOLACUDA_VPT, LOLACUDA_ROWS, LOLACUDA_SYNC, LOLACUDA_EXIT. */
+ * LOLACUDA_BATCH, LOLACUDA_VPT, LOLACUDA_ROWS, LOLACUDA_SYNC, LOLACUDA_EXIT,
+ * LOLACUDA_STAGING. */
 void lolaCudaDefaultConfig(LolaCudaConfig *config);
 
 /* Configuration used by the next lolaCudaPrepare (module API). */
@@ -146,6 +152,8 @@ typedef struct {
   int64_t tilePassesFast;  /* (tile, projection) pairs on the unclamped path */
   int64_t tilePassesSlow;  /* ... on the clamped border path */
   int64_t tilePassesSkipped; /* ... whose footprint misses the detector */
+  int64_t tilePassesStaged;  /* fast-path pairs served from shared-memory staging */
+  int64_t stagedPasses;      /* passes launched with staging */
 } LolaCudaStats;
 
 typedef struct LolaCudaPlan LolaCudaPlan;

@@ -48,7 +48,8 @@ class LolaCudaConfig(C.Structure):
                 ("exitOnError", C.c_int32),
                 ("collectStats", C.c_int32),
                 ("device", C.c_int32),
-                ("reserved", C.c_int32 * 7)]
+                ("staging", C.c_int32),
+                ("reserved", C.c_int32 * 6)]
 
 
 class LolaCudaGeometry(C.Structure):
@@ -66,7 +67,9 @@ class LolaCudaStats(C.Structure):
                 ("passMs", C.c_double),
                 ("tilePassesFast", C.c_int64),
                 ("tilePassesSlow", C.c_int64),
-                ("tilePassesSkipped", C.c_int64)]
+                ("tilePassesSkipped", C.c_int64),
+                ("tilePassesStaged", C.c_int64),
+                ("stagedPasses", C.c_int64)]
 
 
 STORAGE = {"f32": 0, "f16": 1, "bf16": 2, "f32q": 3, "f16q": 4, "bf16q": 5, "tex32": 6,
@@ -172,18 +175,24 @@ def ptr(a: np.ndarray) -> int:
     return a.ctypes.data
 
 
-def config(storage: str = "f32", accumulation: str = "plain", batch: int = 16,
-           voxels_per_thread: int = 8, rows_per_block: int = 8, sync_each_call: int = 1,
-           exit_on_error: int = 0, collect_stats: int = 0, device: int = 0) -> LolaCudaConfig:
+def config(storage: str | None = None, accumulation: str | None = None,
+           batch: int | None = None, voxels_per_thread: int | None = None,
+           rows_per_block: int | None = None, sync_each_call: int | None = None,
+           exit_on_error: int = 0, collect_stats: int | None = None, device: int | None = None,
+           staging: int | None = None) -> LolaCudaConfig:
+    """A LolaCudaConfig from the library's defaults (which honour the
+    LOLACUDA_* environment overrides) with the given fields replaced.
+    exit_on_error defaults to 0 here: Python callers want exceptions."""
     c = LolaCudaConfig()
     load_lolacuda().lolaCudaDefaultConfig(C.byref(c))
-    c.storage = STORAGE[storage]
-    c.accumulation = ACCUM[accumulation]
-    c.batch = batch
-    c.voxelsPerThread = voxels_per_thread
-    c.rowsPerBlock = rows_per_block
-    c.syncEachCall = sync_each_call
-    c.exitOnError = exit_on_error
-    c.collectStats = collect_stats
-    c.device = device
+    if storage is not None:
+        c.storage = STORAGE[storage]
+    if accumulation is not None:
+        c.accumulation = ACCUM[accumulation]
+    for name, value in (("batch", batch), ("voxelsPerThread", voxels_per_thread),
+                        ("rowsPerBlock", rows_per_block), ("syncEachCall", sync_each_call),
+                        ("exitOnError", exit_on_error), ("collectStats", collect_stats),
+                        ("device", device), ("staging", staging)):
+        if value is not None:
+            setattr(c, name, value)
     return c

@@ -71,7 +71,8 @@ def build_lolacuda(force: bool = False, jobs: int | None = None) -> Path:
     cuda = _cuda_home()
     nvcc = str(cuda / "bin" / "nvcc")
     out = LIB / "liblolacuda.so"
-    headers = [CSRC / "bp_kernels.cuh", CSRC / "lolacuda_internal.h", INCLUDE / "lolaCuda.h"]
+    headers = [CSRC / "bp_kernels.cuh", CSRC / "bp_staged.cuh", CSRC / "lolacuda_internal.h",
+               INCLUDE / "lolaCuda.h"]
     common_inc = ["-I" + str(INCLUDE), "-I" + str(CSRC)]
 
     # extra nvcc flags for tuning builds, e.g. LOLACUDA_NVCC_FLAGS=-DLOLA_MIN_BLOCKS=5
@@ -85,12 +86,16 @@ def build_lolacuda(force: bool = False, jobs: int | None = None) -> Path:
                   *extra, *common_inc, "-c", str(src), "-o", str(obj)])
         return obj
 
+    # the host code sees the same tuning defines as the kernels
+    defines = [f for f in extra if f.startswith("-D")]
+
     def compile_c(name: str) -> Path:
         src = CSRC / name
         obj = OBJ / (name + ".o")
         if force or _stale(obj, [src] + headers):
             _run(["gcc", "-O2", "-std=c99", "-fPIC", "-Wall", "-Wextra", "-Wno-unused-parameter",
-                  *common_inc, "-I" + str(cuda / "include"), "-c", str(src), "-o", str(obj)])
+                  *defines, *common_inc, "-I" + str(cuda / "include"), "-c", str(src), "-o",
+                  str(obj)])
         return obj
 
     with ThreadPoolExecutor(max_workers=jobs or min(8, os.cpu_count() or 4)) as ex:

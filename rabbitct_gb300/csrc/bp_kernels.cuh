@@ -596,11 +596,9 @@ int launchPassAccum(const PassArgs &a, const LolaPassParams *P, cudaStream_t str
   return (int)cudaErrorInvalidConfiguration;
 }
 
-template <int S>
-int launchPass(const LolaStoreDesc *st, const LolaPassParams *P, const void *ring, float *volume,
-    unsigned long long *counters, cudaStream_t stream)
+inline void fillPassArgs(PassArgs &a, const LolaStoreDesc *st, const void *ring, float *volume,
+    unsigned long long *counters)
 {
-  PassArgs a;
   a.ring = ring;
   a.slotBytes = st->slotElems * (size_t)st->elemBytes;
   a.volume = volume;
@@ -612,6 +610,14 @@ int launchPass(const LolaStoreDesc *st, const LolaPassParams *P, const void *rin
   a.rows = st->rows;
   for (int i = 0; i < LOLA_MAX_BATCH; ++i)
     a.tex[i] = st->texObjects[i];
+}
+
+template <int S>
+int launchPass(const LolaStoreDesc *st, const LolaPassParams *P, const void *ring, float *volume,
+    unsigned long long *counters, cudaStream_t stream)
+{
+  PassArgs a;
+  fillPassArgs(a, st, ring, volume, counters);
   if (P->accumulation == LOLA_ACCUM_KAHAN)
     return launchPassAccum<S, true>(a, P, stream);
   return launchPassAccum<S, false>(a, P, stream);
@@ -627,8 +633,12 @@ int launchPass(const LolaStoreDesc *st, const LolaPassParams *P, const void *rin
         static_cast<cudaStream_t>(stream));                                                \
   }                                                                                        \
   extern "C" int lolaLaunchPass_##NAME(const LolaStoreDesc *st, const LolaPassParams *P,   \
-      const void *ring, float *volume, unsigned long long *counters, void *stream)         \
+      const LolaStageDesc *sd, const void *ring, float *volume,                            \
+      unsigned long long *counters, void *stream)                                          \
   {                                                                                        \
+    if (sd != nullptr)                                                                     \
+      return lola::launchStaged<S>(st, P, sd, ring, volume, counters,                      \
+          static_cast<cudaStream_t>(stream));                                              \
     return lola::launchPass<S>(st, P, ring, volume, counters,                              \
         static_cast<cudaStream_t>(stream));                                                \
   }

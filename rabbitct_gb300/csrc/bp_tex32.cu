@@ -1,5 +1,5 @@
 /* LolaCUDA kernels instantiated for LOLA_STORE_TEX32 (one translation unit per
  * storage layout so the library's kernels compile in parallel). */
-#include "bp_kernels.cuh"
+#include "bp_staged.cuh"
 
 LOLA_INSTANTIATE_STORAGE(LOLA_STORE_TEX32, TEX32)

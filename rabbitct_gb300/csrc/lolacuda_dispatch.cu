@@ -7,7 +7,7 @@
   extern "C" int lolaLaunchPack_##NAME(const LolaStoreDesc *, const float *, size_t,       \
       void *, int, int, void *);                                                           \
   extern "C" int lolaLaunchPass_##NAME(const LolaStoreDesc *, const LolaPassParams *,      \
-      const void *, float *, unsigned long long *, void *);
+      const LolaStageDesc *, const void *, float *, unsigned long long *, void *);
 
 LOLA_DECLARE(F32)
 LOLA_DECLARE(F16)
@@ -43,23 +43,24 @@ extern "C" int lolaLaunchPack(const LolaStoreDesc *st, const float *d_src, size_
 }
 
 extern "C" int lolaLaunchBackproject(const LolaStoreDesc *st, const LolaPassParams *P,
-    const void *d_ring, float *d_volume, unsigned long long *d_tileCounters, void *stream)
+    const LolaStageDesc *sd, const void *d_ring, float *d_volume,
+    unsigned long long *d_tileCounters, void *stream)
 {
   if (P->count <= 0)
     return 0;
   if (P->count > LOLA_MAX_BATCH)
     return (int)cudaErrorInvalidValue;
   switch (st->storage) {
-  case LOLA_STORE_F32: return lolaLaunchPass_F32(st, P, d_ring, d_volume, d_tileCounters, stream);
-  case LOLA_STORE_F16: return lolaLaunchPass_F16(st, P, d_ring, d_volume, d_tileCounters, stream);
-  case LOLA_STORE_BF16: return lolaLaunchPass_BF16(st, P, d_ring, d_volume, d_tileCounters, stream);
-  case LOLA_STORE_F32Q: return lolaLaunchPass_F32Q(st, P, d_ring, d_volume, d_tileCounters, stream);
-  case LOLA_STORE_F16Q: return lolaLaunchPass_F16Q(st, P, d_ring, d_volume, d_tileCounters, stream);
-  case LOLA_STORE_BF16Q: return lolaLaunchPass_BF16Q(st, P, d_ring, d_volume, d_tileCounters, stream);
-  case LOLA_STORE_TEX32: return lolaLaunchPass_TEX32(st, P, d_ring, d_volume, d_tileCounters, stream);
-  case LOLA_STORE_TEX16: return lolaLaunchPass_TEX16(st, P, d_ring, d_volume, d_tileCounters, stream);
-  case LOLA_STORE_F16QX: return lolaLaunchPass_F16QX(st, P, d_ring, d_volume, d_tileCounters, stream);
-  case LOLA_STORE_F32QX: return lolaLaunchPass_F32QX(st, P, d_ring, d_volume, d_tileCounters, stream);
+  case LOLA_STORE_F32: return lolaLaunchPass_F32(st, P, sd, d_ring, d_volume, d_tileCounters, stream);
+  case LOLA_STORE_F16: return lolaLaunchPass_F16(st, P, sd, d_ring, d_volume, d_tileCounters, stream);
+  case LOLA_STORE_BF16: return lolaLaunchPass_BF16(st, P, sd, d_ring, d_volume, d_tileCounters, stream);
+  case LOLA_STORE_F32Q: return lolaLaunchPass_F32Q(st, P, sd, d_ring, d_volume, d_tileCounters, stream);
+  case LOLA_STORE_F16Q: return lolaLaunchPass_F16Q(st, P, sd, d_ring, d_volume, d_tileCounters, stream);
+  case LOLA_STORE_BF16Q: return lolaLaunchPass_BF16Q(st, P, sd, d_ring, d_volume, d_tileCounters, stream);
+  case LOLA_STORE_TEX32: return lolaLaunchPass_TEX32(st, P, sd, d_ring, d_volume, d_tileCounters, stream);
+  case LOLA_STORE_TEX16: return lolaLaunchPass_TEX16(st, P, sd, d_ring, d_volume, d_tileCounters, stream);
+  case LOLA_STORE_F16QX: return lolaLaunchPass_F16QX(st, P, sd, d_ring, d_volume, d_tileCounters, stream);
+  case LOLA_STORE_F32QX: return lolaLaunchPass_F32QX(st, P, sd, d_ring, d_volume, d_tileCounters, stream);
   default: return (int)cudaErrorInvalidValue;
   }
 }

@@ -20,6 +20,9 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <math.h>
+
+#include <cuda.h>
 #include <cuda_runtime_api.h>
 
 #include "lolaCuda.h"
@@ -116,6 +119,7 @@ void lolaCudaDefaultConfig(LolaCudaConfig *c)
   c->rowsPerBlock = envInt("LOLACUDA_ROWS", c->rowsPerBlock);
   c->syncEachCall = envInt("LOLACUDA_SYNC", c->syncEachCall);
   c->exitOnError = envInt("LOLACUDA_EXIT", c->exitOnError);
+  c->staging = envInt("LOLACUDA_STAGING", 0);
 }
 
 static int validateConfig(const LolaCudaConfig *c)
@@ -176,6 +180,10 @@ struct LolaCudaPlan {
   void *d_ring;
   float *d_stage;
   unsigned long long *d_counters;
+  int *d_error;           /* staged-pass wait timeouts */
+  int stagedLaunched;     /* a staged pass ran since the last error check */
+  LolaStageDesc stageDesc; /* tensor map of the ring for the current box */
+  int stageBoxW, stageBoxH;
   size_t imageElems;
   /* host-staged batch (module API / BackprojectHost) */
   int pending;
@@ -238,6 +246,7 @@ static int planRelease(LolaCudaPlan *p)
   cudaFree(p->d_ring);
   cudaFree(p->d_stage);
   cudaFree(p->d_counters);
+  cudaFree(p->d_error);
   if (p->stageFree)
     cudaEventDestroy(p->stageFree);
   if (p->stageReady)
@@ -320,8 +329,10 @@ static int planInit(LolaCudaPlan *p)
     }
   }
   CUDA_TRY(cudaMalloc((void **)&p->d_stage, (size_t)p->cfg.batch * p->imageElems * sizeof(float)));
-  CUDA_TRY(cudaMalloc((void **)&p->d_counters, 3 * sizeof(unsigned long long)));
-  CUDA_TRY(cudaMemsetAsync(p->d_counters, 0, 3 * sizeof(unsigned long long), p->stream));
+  CUDA_TRY(cudaMalloc((void **)&p->d_counters, 4 * sizeof(unsigned long long)));
+  CUDA_TRY(cudaMemsetAsync(p->d_counters, 0, 4 * sizeof(unsigned long long), p->stream));
+  CUDA_TRY(cudaMalloc((void **)&p->d_error, sizeof(int)));
+  CUDA_TRY(cudaMemsetAsync(p->d_error, 0, sizeof(int), p->stream));
   CUDA_TRY(cudaEventRecord(p->stageFree, p->stream));
   CUDA_TRY(cudaStreamSynchronize(p->stream));
   return 1;
@@ -435,6 +446,181 @@ static int pushEvent(LolaCudaPlan *p, EventPair **out)
   return 1;
 }
 
+
+/* ---- shared-memory staging ------------------------------------------------------
+ * The staged pass copies, per (tile, projection), the box of the stored
+ * projection that the tile's taps fall in.  The box is sized per pass from
+ * the footprints of 27 sample tiles (corners, edge midpoints and centre of the
+ * tile grid) under the pass's matrices; tiles whose footprint exceeds it use
+ * the load path inside the same launch. */
+
+typedef CUresult (*TensorMapEncodeFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
+    const cuuint64_t *, const cuuint64_t *, const cuuint32_t *, const cuuint32_t *,
+    CUtensorMapInterleave, CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static TensorMapEncodeFn tensorMapEncoder(void)
+{
+  static TensorMapEncodeFn fn = NULL;
+  static int tried = 0;
+  if (!tried) {
+    tried = 1;
+    void *f = NULL;
+    enum cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault,
+            &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (TensorMapEncodeFn)f;
+  }
+  return fn;
+}
+
+/* Tensor-map element type, elements per stored pixel and bytes per pixel. */
+static int stageFormat(int storage, CUtensorMapDataType *dt, int *epp, int *pix)
+{
+  switch (storage) {
+  case LOLA_STORE_F32: *dt = CU_TENSOR_MAP_DATA_TYPE_FLOAT32; *epp = 1; *pix = 4; return 1;
+  case LOLA_STORE_F16:
+  case LOLA_STORE_BF16: *dt = CU_TENSOR_MAP_DATA_TYPE_UINT16; *epp = 1; *pix = 2; return 1;
+  case LOLA_STORE_F32Q:
+  case LOLA_STORE_F32QX: *dt = CU_TENSOR_MAP_DATA_TYPE_UINT64; *epp = 2; *pix = 16; return 1;
+  case LOLA_STORE_F16Q:
+  case LOLA_STORE_F16QX:
+  case LOLA_STORE_BF16Q: *dt = CU_TENSOR_MAP_DATA_TYPE_UINT64; *epp = 1; *pix = 8; return 1;
+  default: return 0;
+  }
+}
+
+/* per stage; LOLA_STAGES of them share about 72 KB per block */
+#define LOLA_STAGE_MAX_BYTES (72 * 1024 / LOLA_STAGES)
+
+/* Box (pixels) that holds the taps of the sampled tiles; 0 if nothing fits. */
+static void sampleFootprint(const LolaCudaPlan *p, const double *mats, int count, int *needW,
+    int *needH)
+{
+  const int N = p->geom.problemSize;
+  const int TX = 32, TY = p->cfg.rowsPerBlock, TZ = p->cfg.voxelsPerThread;
+  const int nt[3] = { (N + TX - 1) / TX, (N + TY - 1) / TY, (N + TZ - 1) / TZ };
+  const int te[3] = { TX, TY, TZ };
+  const double vs = (double)p->geom.voxelSize, o = (double)p->geom.originIndex;
+  const double W = p->geom.imageWidth, H = p->geom.imageHeight;
+  int mw = 0, mh = 0;
+  for (int q = 0; q < count; q++) {
+    const double *a = mats + 12 * (size_t)q;
+    for (int t = 0; t < 27; t++) {
+      int org[3], ext[3];
+      int tt = t;
+      for (int d = 0; d < 3; d++) {
+        const int sel = tt % 3;
+        tt /= 3;
+        const int ti = sel == 0 ? 0 : (sel == 1 ? nt[d] / 2 : nt[d] - 1);
+        org[d] = ti * te[d];
+        ext[d] = (org[d] + te[d] <= N ? te[d] : N - org[d]) - 1;
+      }
+      double mnu = 1e30, mxu = -1e30, mnv = 1e30, mxv = -1e30;
+      int bad = 0;
+      for (int c = 0; c < 8; c++) {
+        const double X = o + (double)(org[0] + ((c & 1) ? ext[0] : 0)) * vs;
+        const double Y = o + (double)(org[1] + ((c & 2) ? ext[1] : 0)) * vs;
+        const double Z = o + (double)(org[2] + ((c & 4) ? ext[2] : 0)) * vs;
+        const double w = a[2] * X + a[5] * Y + a[8] * Z + a[11];
+        if (!(w > 0.0)) {
+          bad = 1;
+          break;
+        }
+        const double u = (a[0] * X + a[3] * Y + a[6] * Z + a[9]) / w;
+        const double v = (a[1] * X + a[4] * Y + a[7] * Z + a[10]) / w;
+        mnu = u < mnu ? u : mnu;
+        mxu = u > mxu ? u : mxu;
+        mnv = v < mnv ? v : mnv;
+        mxv = v > mxv ? v : mxv;
+      }
+      if (bad || mxu <= -2.0 || mnu >= W || mxv <= -2.0 || mnv >= H)
+        continue;
+      const int w = (int)(floor(mxu + 0.5) - floor(mnu - 0.5)) + 3;
+      const int h = (int)(floor(mxv + 0.5) - floor(mnv - 0.5)) + 3;
+      mw = w > mw ? w : mw;
+      mh = h > mh ? h : mh;
+    }
+  }
+  *needW = mw;
+  *needH = mh;
+}
+
+/* Fills p->stageDesc for this pass; returns 1 if the pass should be staged. */
+static int prepareStage(LolaCudaPlan *p, const double *mats, int count)
+{
+  if (!p->cfg.staging)
+    return 0;
+  /* staged kernels are compiled for 8 voxels per thread and 4 or 8 rows */
+  if (p->cfg.voxelsPerThread != 8 || (p->cfg.rowsPerBlock != 8 && p->cfg.rowsPerBlock != 4))
+    return 0;
+  CUtensorMapDataType dt;
+  int epp, pix;
+  if (!stageFormat(p->store.storage, &dt, &epp, &pix))
+    return 0;
+  TensorMapEncodeFn encode = tensorMapEncoder();
+  if (encode == NULL)
+    return 0;
+  int needW, needH;
+  sampleFootprint(p, mats, count, &needW, &needH);
+  if (needW <= 0 || needH <= 0)
+    return 0;
+  const int align = pix >= 16 ? 1 : 16 / pix;
+  /* 10 % headroom over the sampled maximum, plus the alignment slack */
+  int bw = ((needW + needW / 10 + 2 * align - 1) / align) * align;
+  int bh = needH + needH / 10 + 1;
+  const int maxW = (256 / epp / align) * align;
+  if (bw > maxW)
+    bw = maxW;
+  if (bh > 256)
+    bh = 256;
+  while ((long)bw * bh * pix > LOLA_STAGE_MAX_BYTES && bh > 8)
+    bh--;
+  /* a box smaller than the sampled footprints would send most tiles down the
+     load path anyway: stage only when the sampled tiles fit */
+  if (bw < needW + align - 1 || bh < needH)
+    return 0;
+  if (bw != p->stageBoxW || bh != p->stageBoxH) {
+    const LolaStoreDesc *st = &p->store;
+    cuuint64_t dims[3] = { (cuuint64_t)st->pitch * epp, (cuuint64_t)st->rows,
+      (cuuint64_t)p->cfg.batch };
+    cuuint64_t strides[2] = { (cuuint64_t)st->pitch * pix, (cuuint64_t)st->slotElems * pix };
+    cuuint32_t box[3] = { (cuuint32_t)(bw * epp), (cuuint32_t)bh, 1 };
+    cuuint32_t estr[3] = { 1, 1, 1 };
+    CUresult r = encode(&p->stageDesc.tensorMap, dt, 3, p->d_ring, dims, strides, box, estr,
+        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+        CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS)
+      return 0;
+    p->stageBoxW = bw;
+    p->stageBoxH = bh;
+  }
+  LolaStageDesc *sd = &p->stageDesc;
+  sd->boxW = bw;
+  sd->boxH = bh;
+  sd->align = align;
+  sd->elemsPerPixel = epp;
+  sd->boxBytes = bw * bh * pix;
+  sd->stageBytes = (sd->boxBytes + 127) & ~127;
+  sd->d_error = p->d_error;
+  return 1;
+}
+
+/* Reports (and clears) a wait timeout recorded by a staged pass. */
+static int checkStageError(LolaCudaPlan *p)
+{
+  if (!p->stagedLaunched)
+    return 1;
+  p->stagedLaunched = 0;
+  int e = 0;
+  CUDA_TRY(cudaMemcpy(&e, p->d_error, sizeof(int), cudaMemcpyDeviceToHost));
+  if (e != 0) {
+    CUDA_TRY(cudaMemset(p->d_error, 0, sizeof(int)));
+    return setError("staged pass: a shared-memory stage wait timed out (code %d)", e);
+  }
+  return 1;
+}
+
 /* One backprojection pass over ring slots [0, count) with the given matrices. */
 static int launchPass(LolaCudaPlan *p, const double *mats, int count)
 {
@@ -456,8 +642,13 @@ static int launchPass(LolaCudaPlan *p, const double *mats, int count)
       return 0;
     CUDA_TRY(cudaEventRecord(ev->start, p->stream));
   }
-  LAUNCH_TRY(lolaLaunchBackproject(&p->store, &P, p->d_ring, p->d_volume,
-      p->cfg.collectStats ? p->d_counters : NULL, p->stream));
+  const int staged = prepareStage(p, mats, count);
+  LAUNCH_TRY(lolaLaunchBackproject(&p->store, &P, staged ? &p->stageDesc : NULL, p->d_ring,
+      p->d_volume, p->cfg.collectStats ? p->d_counters : NULL, p->stream));
+  if (staged) {
+    p->stagedLaunched = 1;
+    p->stats.stagedPasses++;
+  }
   if (ev != NULL)
     CUDA_TRY(cudaEventRecord(ev->stop, p->stream));
   p->stats.passes++;
@@ -559,7 +750,7 @@ int lolaCudaPlanSynchronize(LolaCudaPlan *p)
     return 0;
   CUDA_TRY(cudaStreamSynchronize(p->copyStream));
   CUDA_TRY(cudaStreamSynchronize(p->stream));
-  return 1;
+  return checkStageError(p);
 }
 
 int lolaCudaPlanTimerStart(LolaCudaPlan *p)
@@ -592,11 +783,12 @@ int lolaCudaPlanGetStats(LolaCudaPlan *p, LolaCudaStats *out)
     return 0;
   if (!collectEvents(p))
     return 0;
-  unsigned long long c[3] = { 0, 0, 0 };
+  unsigned long long c[4] = { 0, 0, 0, 0 };
   CUDA_TRY(cudaMemcpy(c, p->d_counters, sizeof(c), cudaMemcpyDeviceToHost));
   p->stats.tilePassesSkipped = (int64_t)c[0];
   p->stats.tilePassesFast = (int64_t)c[1];
   p->stats.tilePassesSlow = (int64_t)c[2];
+  p->stats.tilePassesStaged = (int64_t)c[3];
   *out = p->stats;
   return 1;
 }
@@ -608,7 +800,7 @@ int lolaCudaPlanResetStats(LolaCudaPlan *p)
   if (!lolaCudaPlanSynchronize(p) || !collectEvents(p))
     return 0;
   memset(&p->stats, 0, sizeof(p->stats));
-  CUDA_TRY(cudaMemset(p->d_counters, 0, 3 * sizeof(unsigned long long)));
+  CUDA_TRY(cudaMemset(p->d_counters, 0, 4 * sizeof(unsigned long long)));
   return 1;
 }
 
@@ -746,6 +938,8 @@ int lolaCudaBackprojection(RabbitCtGlobalData *d)
       setError("pass failed: %s", cudaGetErrorString(e));
       return moduleFail("backprojection");
     }
+    if (!checkStageError(p))
+      return moduleFail("backprojection");
   }
   return 1;
 }

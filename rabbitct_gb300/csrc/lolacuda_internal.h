@@ -6,6 +6,8 @@
 #include <stddef.h>
 #include <stdint.h>
 
+#include <cuda.h>
+
 #include "lolaCuda.h"
 
 #ifdef __cplusplus
@@ -53,13 +55,32 @@ typedef struct {
   LolaPassProj proj[LOLA_MAX_BATCH];
 } LolaPassParams;
 
+/* Stage buffers of the staged pass (a build-time tuning knob). */
+#ifndef LOLA_STAGES
+#define LOLA_STAGES 3
+#endif
+
+/* Shared-memory staging of one pass (bp_staged.cuh): the tensor map over the
+ * stored ring and the staging box. */
+typedef struct {
+  CUtensorMap tensorMap;  /* 3D: {pixel elements, rows, slots} */
+  int32_t boxW, boxH;     /* staging box, pixels */
+  int32_t align;          /* box origin alignment, pixels */
+  int32_t elemsPerPixel;  /* tensor elements per stored pixel */
+  int32_t stageBytes;     /* one stage buffer, 128 B multiple */
+  int32_t boxBytes;       /* bytes one tensor copy delivers */
+  int *d_error;           /* device flag set on a wait timeout */
+} LolaStageDesc;
+
 /* Kernel launchers (lolacuda_dispatch.cu).  Return 0 on success or a
  * cudaError_t value. */
 int lolaLaunchPack(const LolaStoreDesc *store, const float *d_src, size_t srcStride,
     void *d_ring, int slot0, int count, void *stream);
 
+/* stage = NULL: load-path pass; otherwise the TMA-staged pass. */
 int lolaLaunchBackproject(const LolaStoreDesc *store, const LolaPassParams *params,
-    const void *d_ring, float *d_volume, unsigned long long *d_tileCounters, void *stream);
+    const LolaStageDesc *stage, const void *d_ring, float *d_volume,
+    unsigned long long *d_tileCounters, void *stream);
 
 /* Sets the thread's lolaCudaLastError() message; returns 0. */
 int lolaSetError(const char *fmt, ...);

@@ -163,7 +163,7 @@ extern "C" int lolaCudaBackprojectNoAlloc(const LolaCudaGeometry *g, const LolaC
       pp.slot = i;
       pp.reserved[0] = pp.reserved[1] = pp.reserved[2] = 0;
     }
-    rc = lolaLaunchBackproject(&st, &P, ring, d_volume, nullptr, stream);
+    rc = lolaLaunchBackproject(&st, &P, nullptr, ring, d_volume, nullptr, stream);
     if (rc != 0)
       return lolaSetError("pass launch failed: %s", cudaGetErrorString((cudaError_t)rc));
     done += n;
