@@ -216,7 +216,7 @@ def test_staged_pass_ragged_volume_and_rows(lib):
     o = synth.origin_index(n, vs)
     ref = oracle.bunny_f64(n, vs, o, scan.matrices, scan.images)
     with Plan(n, vs, o, scan.width, scan.height, storage="f32", batch=10, rows_per_block=4,
-              collect_stats=1) as plan:
+              collect_stats=1, staging=1) as plan:
         plan.backproject_host(scan.images, scan.matrices)
         vol = plan.download()
         st = plan.stats()
