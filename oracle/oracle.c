@@ -110,6 +110,34 @@ void oracleBunnyF32(int N, float voxelSize, float originIndex, int W, int H, int
   }
 }
 
+/* LolaBunny at selected voxels only (flattened indices k*N*N + j*N + i), for
+ * error statistics of full-size volumes.  fp32Accumulate = 0 sums in FP64;
+ * 1 accumulates (float)(term) per view in FP32 like src/LolaBunny.c:68.
+ * out[q] starts from zero. */
+void oracleBunnyPoints(int N, float voxelSize, float originIndex, int W, int H, int nproj,
+    const double *mats, const float *images, int npts, const int64_t *index, int fp32Accumulate,
+    double *out)
+{
+  const size_t img = (size_t)W * (size_t)H;
+  const int64_t NN = (int64_t)N * N;
+#pragma omp parallel for schedule(dynamic, 16)
+  for (int q = 0; q < npts; q++) {
+    const int64_t id = index[q];
+    const int k = (int)(id / NN), j = (int)((id / N) % N), i = (int)(id % N);
+    const double x = (double)originIndex + (double)i * (double)voxelSize;
+    const double y = (double)originIndex + (double)j * (double)voxelSize;
+    const double z = (double)originIndex + (double)k * (double)voxelSize;
+    double acc = 0.0;
+    float acc32 = 0.0f;
+    for (int p = 0; p < nproj; p++) {
+      const double t = bunnyTerm(mats + 12 * (size_t)p, images + img * p, W, H, x, y, z);
+      acc += t;
+      acc32 += (float)t;
+    }
+    out[q] = fp32Accumulate ? (double)acc32 : acc;
+  }
+}
+
 /* ---- geometry analysis ---------------------------------------------------- */
 
 /* shadow[4] = {Umin, Umax, Vmin, Vmax} of the 8 volume corners over all views */

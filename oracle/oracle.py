@@ -47,6 +47,8 @@ def lib() -> C.CDLL:
         L.oracleOptBackproject.argtypes = [C.c_int, C.c_float, C.c_float, C.c_int, _P, _P, _P,
                                            C.c_int, C.c_int, _P, _P]
         L.oracleOptBackproject.restype = None
+        L.oracleBunnyPoints.argtypes = geo + [_P, C.c_int, _P, C.c_int, _P]
+        L.oracleBunnyPoints.restype = None
         L.oracleThreads.argtypes = []
         L.oracleThreads.restype = C.c_int
         _lib = L
@@ -74,6 +76,17 @@ def bunny_f32(n, vs, o, mats, images, vol=None) -> np.ndarray:
     mats, images, g = _geo(n, vs, o, mats, images)
     out = np.zeros((n, n, n), np.float32) if vol is None else vol
     lib().oracleBunnyF32(*g, images.ctypes.data, out.ctypes.data)
+    return out
+
+
+def bunny_points(n, vs, o, mats, images, index, fp32_accumulate=False) -> np.ndarray:
+    """LolaBunny at the flattened voxel indices `index` (FP64 sums, or FP32
+    accumulation like the reference)."""
+    mats, images, g = _geo(n, vs, o, mats, images)
+    idx = np.ascontiguousarray(index, np.int64)
+    out = np.zeros(idx.size, np.float64)
+    lib().oracleBunnyPoints(*g, images.ctypes.data, idx.size, idx.ctypes.data,
+                            int(fp32_accumulate), out.ctypes.data)
     return out
 
 
