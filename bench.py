@@ -66,7 +66,7 @@ def parse_args():
     ap.add_argument("--nproj", type=int, default=496)
     ap.add_argument("--width", type=int, default=1248)
     ap.add_argument("--height", type=int, default=960)
-    ap.add_argument("--storage", default="f16q", choices=list(STORAGE_IDS))
+    ap.add_argument("--storage", default="f16qx", choices=list(STORAGE_IDS))
     ap.add_argument("--fp32-storage", default="f32", choices=list(STORAGE_IDS))
     ap.add_argument("--batch", type=int, default=16)
     ap.add_argument("--vpt", type=int, default=8)
