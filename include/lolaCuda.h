@@ -193,6 +193,20 @@ int lolaCudaPlanTimerStop(LolaCudaPlan *plan, double *ms);
 int lolaCudaPlanGetStats(LolaCudaPlan *plan, LolaCudaStats *stats);
 int lolaCudaPlanResetStats(LolaCudaPlan *plan);
 
+/* ---- Geometry analysis on the device ----------------------------------------
+ * Replaces computeLineRanges (src/analyseGeometry.c:102-298) for the
+ * reference's clipping modules: range[view] (view < data->numberOfProjections,
+ * from data->globalGeometry) receives N*N {start, stop} int16 pairs for rows
+ * z*N + y, identical to the reference's table for the same vectorSize
+ * (VECTORSIZE there).  signedHit = 0 keeps the reference's hit test (its
+ * unsigned comparison counts pixel index -1 as a miss); 1 keeps every voxel
+ * LolaBunny reads a non-zero tap for.  No cache file is read or written. */
+int lolaCudaComputeLineRanges(const RabbitCtGlobalData *data, int16_t **range, int vectorSize,
+    int signedHit);
+/* computeShadowOfProjection (src/analyseGeometry.c:50-93): shadow[4] =
+ * {Umin, Umax, Vmin, Vmax}. */
+int lolaCudaComputeShadow(const RabbitCtGlobalData *data, int *shadow);
+
 /* ---- Backprojection without device allocation ------------------------------
  * No counterpart in the reference (its modules are CPU code).  For callers
  * that cannot allocate device memory while they run — an acquisition loop

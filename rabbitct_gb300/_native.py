@@ -110,6 +110,9 @@ _SIGNATURES = [
     ("lolaCudaBackprojectNoAlloc", C.c_int, [C.POINTER(LolaCudaGeometry),
                                              C.POINTER(LolaCudaConfig), _P, _P, C.c_size_t,
                                              _P, C.c_int, _P]),
+    ("lolaCudaComputeLineRanges", C.c_int, [C.POINTER(RabbitCtGlobalData), _P, C.c_int,
+                                            C.c_int]),
+    ("lolaCudaComputeShadow", C.c_int, [C.POINTER(RabbitCtGlobalData), _P]),
     ("lolaCudaHostAlloc", _P, [C.c_size_t]),
     ("lolaCudaHostFree", C.c_int, [_P]),
     ("lolaCudaProbeIssueRate", C.c_double, []),
