@@ -76,6 +76,9 @@ def parse_args():
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--cpu-views", type=int, default=8,
                     help="projections in the bounded CPU-baseline sample")
+    ap.add_argument("--shard", default="slabs", choices=["slabs", "replicas"],
+                    help="N>1: z-slabs of one volume per GPU (strong scaling) or one "
+                         "whole reconstruction per GPU (weak scaling)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp32", action="store_true")
@@ -232,7 +235,7 @@ def run_reference(args, rank, world):
         "impl": "reference", "metric": METRIC, "value": value, "unit": "GUPS",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": args.n ** 3 * min(args.cpu_views, scan.nproj) / value / 1e6,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "higher_is_better": True, "scaling": "strong" if args.shard == "slabs" else "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded ellipsoid phantom, RabbitCT shapes)",
         "config": workload_config(args, "f32"),
         "cpu_baseline": {k: res[k] for k in ("value", "unit", "cores", "kind", "sample")},
@@ -252,19 +255,35 @@ def workload_config(args, storage):
             "detector": f"{args.width}x{args.height}", "storage": storage,
             "batch": args.batch, "voxels_per_thread": args.vpt, "rows_per_block": args.rows,
             "l2": "inputs larger than L2 (volume and projections each exceed 129 MB)",
-            "parallelism": "replicas (one full reconstruction per GPU)"}
+            "parallelism": ("z-slabs of one volume, one per GPU, no collective"
+                            if args.shard == "slabs" else
+                            "replicas (one full reconstruction per GPU)")}
 
 
 # ---------------------------------------------------------------------------
 # GPU arm
 # ---------------------------------------------------------------------------
 
+def my_slab(args, dist):
+    """z-slab of this rank: all of the volume unless sharding by slabs."""
+    from rabbitct_gb300.lolacuda import slab
+    if args.shard == "slabs" and dist.world > 1:
+        return slab(args.n, dist.rank, dist.world, args.vpt)
+    return (0, args.n)
+
+
+def total_updates(args, scan, dist) -> float:
+    """Voxel updates of one step over all ranks."""
+    per = float(args.n) ** 3 * scan.nproj
+    return per if args.shard == "slabs" else per * dist.world
+
+
 def time_device(args, dist, lib_mod, scan, vs, o, d_images, storage, clocks=None):
     from rabbitct_gb300.lolacuda import Plan
     W, H = scan.width, scan.height
     with Plan(args.n, vs, o, W, H, storage=storage, batch=args.batch,
               voxels_per_thread=args.vpt, rows_per_block=args.rows, collect_stats=1,
-              staging=args.staging) as p:
+              staging=args.staging, slab=my_slab(args, dist)) as p:
         for _ in range(args.warmup):
             p.zero()
             p.backproject_device(d_images.ptr, W * H, scan.matrices)
@@ -284,7 +303,7 @@ def time_device(args, dist, lib_mod, scan, vs, o, d_images, storage, clocks=None
         dist.barrier()
         st = p.stats()
     ms_max = dist.max(ms)
-    updates = float(args.n) ** 3 * scan.nproj * args.steps * dist.world
+    updates = total_updates(args, scan, dist) * args.steps
     return {"ms": ms_max, "gups": updates / (ms_max * 1e-3) / 1e9, "stats": st, "clocks": clk}
 
 
@@ -329,9 +348,48 @@ def roofline(args, lib, storage, st, probes) -> dict:
     return out
 
 
+def time_e2e_slab(args, dist, scan, vs, o, storage) -> dict:
+    """N>1 with slabs: the plan API from pinned host buffers, each rank
+    uploading every projection and reading its slab back."""
+    import ctypes as C
+
+    from rabbitct_gb300._native import load_lolacuda
+    from rabbitct_gb300.lolacuda import Plan
+    lib = load_lolacuda()
+    n, W, H = args.n, scan.width, scan.height
+    b, c = my_slab(args, dist)
+    nbytes_img = 4 * W * H * scan.nproj
+    hi = lib.lolaCudaHostAlloc(nbytes_img)
+    hv = lib.lolaCudaHostAlloc(max(4, 4 * n * n * c))
+    imgs = np.ctypeslib.as_array((C.c_float * (W * H * scan.nproj)).from_address(hi))
+    imgs = imgs.reshape(scan.nproj, H, W)
+    imgs[...] = scan.images
+    vol = np.ctypeslib.as_array((C.c_float * max(1, n * n * c)).from_address(hv))
+    times = []
+    for step in range(1 + args.e2e_steps):
+        dist.barrier()
+        t0 = time.perf_counter()
+        with Plan(n, vs, o, W, H, storage=storage, batch=args.batch, voxels_per_thread=args.vpt,
+                  rows_per_block=args.rows, staging=args.staging, slab=(b, c)) as p:
+            p.backproject_host(imgs, scan.matrices)
+            p.download(vol[:n * n * c].reshape(c, n, n))
+        dt = time.perf_counter() - t0
+        dist.barrier()
+        if step > 0:
+            times.append(dist.max(dt))
+    lib.lolaCudaHostFree(hi)
+    lib.lolaCudaHostFree(hv)
+    t = statistics.median(times)
+    return {"value": total_updates(args, scan, dist) / t / 1e9, "unit": "GUPS", "seconds": t,
+            "h2d_bytes_per_step": nbytes_img, "d2h_bytes_per_step": 4 * n * n * c,
+            "path": "plan API per z-slab, pinned host"}
+
+
 def time_e2e(args, dist, scan, vs, o, storage) -> dict:
     """Module API (prepare / backprojection per projection / finish) with
     pinned host buffers, as rabbitRunner drives a module with -b 1 -a."""
+    if args.shard == "slabs" and dist.world > 1:
+        return time_e2e_slab(args, dist, scan, vs, o, storage)
     import ctypes as C
 
     from rabbitct_gb300._native import check, config, load_lolacuda
@@ -376,7 +434,7 @@ def time_e2e(args, dist, scan, vs, o, storage) -> dict:
     lib.lolaCudaHostFree(hv)
     lib.lolaCudaHostFree(hi)
     t = statistics.median(times)
-    gups = float(n) ** 3 * scan.nproj * dist.world / t / 1e9
+    gups = total_updates(args, scan, dist) / t / 1e9
     return {"value": gups, "unit": "GUPS", "seconds": t,
             "h2d_bytes_per_step": nbytes_vol + nbytes_img,
             "d2h_bytes_per_step": nbytes_vol, "path": "module API, -b 1 calls, pinned host",
@@ -419,7 +477,8 @@ def run_gpu(args, rank, world, local):
         "metric": METRIC, "value": head["gups"], "unit": "GUPS", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": head["ms"] / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "scaling": "strong" if args.shard == "slabs" else "weak", "vs_baseline": None,
+        "dtype": "f32",
         "data": "synthetic (seeded ellipsoid phantom, RabbitCT shapes)",
         "config": workload_config(args, args.storage),
         "gpu_launches": int(st.passes + st.packs),

@@ -142,6 +142,13 @@ typedef struct {
   int32_t imageHeight;
   float voxelSize;
   float originIndex;     /* O_Index */
+  /* z-slab held by the plan: slices [sliceBegin, sliceBegin + sliceCount) of
+     the N^3 volume (sliceCount 0 = the whole volume).  Slabs let several GPUs
+     share one volume with no exchange: each backprojects every projection
+     into its own slab.  Slabs starting at multiples of the tile depth
+     (voxelsPerThread) give bit-identical voxels to an unsharded plan. */
+  int32_t sliceBegin;
+  int32_t sliceCount;
 } LolaCudaGeometry;
 
 typedef struct {
@@ -163,7 +170,7 @@ int lolaCudaPlanCreate(const LolaCudaGeometry *geometry, const LolaCudaConfig *c
     LolaCudaPlan **plan);
 int lolaCudaPlanDestroy(LolaCudaPlan *plan);
 
-/* Device pointer of the N^3 FP32 volume (x fastest). */
+/* Device pointer of the plan's FP32 volume, N x N x sliceCount, x fastest. */
 float *lolaCudaPlanVolume(LolaCudaPlan *plan);
 /* cudaStream_t the plan launches on. */
 void *lolaCudaPlanStream(LolaCudaPlan *plan);
@@ -193,6 +200,25 @@ int lolaCudaPlanTimerStop(LolaCudaPlan *plan, double *ms);
 int lolaCudaPlanGetStats(LolaCudaPlan *plan, LolaCudaStats *stats);
 int lolaCudaPlanResetStats(LolaCudaPlan *plan);
 
+/* ---- Verification on the device ------------------------------------------------
+ * The runner's -c check (src/rabbitRunner.c:320-384) without copying the
+ * volume to the host: HU = floor(hus[0] * v + hus[1] + 0.5) for v > 0 else 0,
+ * clamped to 4095, against a uint16 HU reference volume (host memory, N^3).
+ * With convertInPlace the HU values replace the volume, as the runner does
+ * before it writes -o. */
+typedef struct {
+  double mse;              /* HU^2 */
+  double rmse;             /* HU */
+  double maxAbs;           /* HU */
+  double psnr;             /* dB, 10 log10(4095^2 / mse); inf when mse <= 1e-8 */
+  uint64_t histogram[11];  /* |error| in [0,1), [1,2), ..., [9,10), >= 10 */
+} LolaCudaQuality;
+
+int lolaCudaVerifyVolume(float *d_volume, size_t voxels, const uint16_t *h_reference,
+    const float *hus, int convertInPlace, void *stream, LolaCudaQuality *quality);
+int lolaCudaPlanVerify(LolaCudaPlan *plan, const uint16_t *h_reference, const float *hus,
+    int convertInPlace, LolaCudaQuality *quality);
+
 /* ---- Geometry analysis on the device ----------------------------------------
  * Replaces computeLineRanges (src/analyseGeometry.c:102-298) for the
  * reference's clipping modules: range[view] (view < data->numberOfProjections,
@@ -206,6 +232,11 @@ int lolaCudaComputeLineRanges(const RabbitCtGlobalData *data, int16_t **range, i
 /* computeShadowOfProjection (src/analyseGeometry.c:50-93): shadow[4] =
  * {Umin, Umax, Vmin, Vmax}. */
 int lolaCudaComputeShadow(const RabbitCtGlobalData *data, int *shadow);
+
+/* Slab of `rank` among `ranks` for an N^3 volume: near-equal counts, starts at
+ * multiples of `align` (the tile depth) so voxels match an unsharded plan. */
+int lolaCudaSlab(int problemSize, int rank, int ranks, int align, int32_t *sliceBegin,
+    int32_t *sliceCount);
 
 /* ---- Backprojection without device allocation ------------------------------
  * No counterpart in the reference (its modules are CPU code).  For callers

@@ -57,7 +57,14 @@ class LolaCudaGeometry(C.Structure):
                 ("imageWidth", C.c_int32),
                 ("imageHeight", C.c_int32),
                 ("voxelSize", C.c_float),
-                ("originIndex", C.c_float)]
+                ("originIndex", C.c_float),
+                ("sliceBegin", C.c_int32),
+                ("sliceCount", C.c_int32)]
+
+
+class LolaCudaQuality(C.Structure):
+    _fields_ = [("mse", C.c_double), ("rmse", C.c_double), ("maxAbs", C.c_double),
+                ("psnr", C.c_double), ("histogram", C.c_uint64 * 11)]
 
 
 class LolaCudaStats(C.Structure):
@@ -113,6 +120,11 @@ _SIGNATURES = [
     ("lolaCudaComputeLineRanges", C.c_int, [C.POINTER(RabbitCtGlobalData), _P, C.c_int,
                                             C.c_int]),
     ("lolaCudaComputeShadow", C.c_int, [C.POINTER(RabbitCtGlobalData), _P]),
+    ("lolaCudaVerifyVolume", C.c_int, [_P, C.c_size_t, _P, _P, C.c_int, _P,
+                                       C.POINTER(LolaCudaQuality)]),
+    ("lolaCudaPlanVerify", C.c_int, [_P, _P, _P, C.c_int, C.POINTER(LolaCudaQuality)]),
+    ("lolaCudaSlab", C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int32),
+                               C.POINTER(C.c_int32)]),
     ("lolaCudaHostAlloc", _P, [C.c_size_t]),
     ("lolaCudaHostFree", C.c_int, [_P]),
     ("lolaCudaProbeIssueRate", C.c_double, []),

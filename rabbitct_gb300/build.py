@@ -27,7 +27,7 @@ CU_SOURCES = [
     "bp_f32.cu", "bp_f16.cu", "bp_bf16.cu", "bp_f32q.cu", "bp_f16q.cu", "bp_bf16q.cu",
     "bp_tex32.cu", "bp_tex16.cu", "bp_f16qx.cu", "bp_f32qx.cu",
     "lolacuda_dispatch.cu", "lolacuda_probe.cu", "lolacuda_noalloc.cu",
-    "lolacuda_geometry.cu",
+    "lolacuda_geometry.cu", "lolacuda_verify.cu",
 ]
 C_SOURCES = ["lolacuda_host.c"]
 

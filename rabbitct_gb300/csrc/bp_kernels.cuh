@@ -429,7 +429,8 @@ __device__ __forceinline__ void setupTile(const LolaPassParams &P, const PassArg
   __syncthreads();
 
   /* -- setup B: footprint of the tile from its 8 corners, 8 lanes per view -- */
-  const int ex = min(32, N - x0) - 1, ey = min(ROWS, N - y0) - 1, ez = min(VPT, N - z0) - 1;
+  const int ex = min(32, N - x0) - 1, ey = min(ROWS, N - y0) - 1;
+  const int ez = min(VPT, P.zEnd - z0) - 1;
   for (int base = 0; base < 8 * count; base += nthreads) {
     const int t = base + tid;
     const bool active = t < 8 * count;
@@ -500,7 +501,7 @@ __global__ void __launch_bounds__(32 * ROWS, LOLA_PASS_MIN_BLOCKS(VPT, ROWS))
 {
   __shared__ TileProj sp[LOLA_MAX_BATCH];
   const int N = P.N;
-  const int x0 = blockIdx.x * 32, y0 = blockIdx.y * ROWS, z0 = blockIdx.z * VPT;
+  const int x0 = blockIdx.x * 32, y0 = blockIdx.y * ROWS, z0 = P.zBegin + blockIdx.z * VPT;
   const int tid = threadIdx.y * 32 + threadIdx.x;
   const int count = P.count;
 
@@ -523,11 +524,13 @@ __global__ void __launch_bounds__(32 * ROWS, LOLA_PASS_MIN_BLOCKS(VPT, ROWS))
   const int x = x0 + threadIdx.x, y = y0 + threadIdx.y;
   const bool inXY = (x < N) && (y < N);
   const size_t slice = (size_t)N * (size_t)N;
-  float *vcol = a.volume + ((size_t)z0 * N + (size_t)(inXY ? y : 0)) * (size_t)N + (inXY ? x : 0);
+  /* the plan holds only the slab z in [zBegin, zEnd) */
+  float *vcol = a.volume + ((size_t)(z0 - P.zBegin) * N + (size_t)(inXY ? y : 0)) * (size_t)N +
+                (inXY ? x : 0);
   float acc[VPT], comp[VPT];
 #pragma unroll
   for (int k = 0; k < VPT; ++k) {
-    acc[k] = (inXY && z0 + k < N) ? vcol[k * slice] : 0.0f;
+    acc[k] = (inXY && z0 + k < P.zEnd) ? vcol[k * slice] : 0.0f;
     comp[k] = 0.0f;
   }
   const float fi = (float)threadIdx.x, fj = (float)threadIdx.y;
@@ -546,7 +549,7 @@ __global__ void __launch_bounds__(32 * ROWS, LOLA_PASS_MIN_BLOCKS(VPT, ROWS))
   }
 #pragma unroll
   for (int k = 0; k < VPT; ++k) {
-    if (inXY && z0 + k < N)
+    if (inXY && z0 + k < P.zEnd)
       vcol[k * slice] = KAHAN ? (acc[k] - comp[k]) : acc[k];
   }
 }
@@ -579,7 +582,8 @@ int launchPassShape(const PassArgs &a, const LolaPassParams *P, cudaStream_t str
 {
   const int N = P->N;
   const dim3 block(32, ROWS);
-  const dim3 grid((N + 31) / 32, (N + ROWS - 1) / ROWS, (N + VPT - 1) / VPT);
+  const int nz = P->zEnd - P->zBegin;
+  const dim3 grid((N + 31) / 32, (N + ROWS - 1) / ROWS, (nz + VPT - 1) / VPT);
   passKernel<S, VPT, ROWS, KAHAN><<<grid, block, 0, stream>>>(a, *P);
   return (int)cudaGetLastError();
 }

@@ -245,7 +245,7 @@ __global__ void __launch_bounds__(32 * (ROWS + 1), LOLA_STAGED_MIN_BLOCKS)
   __shared__ __align__(8) unsigned long long bars[2 * NS]; /* full[NS], empty[NS] */
   const int N = P.N;
   const int count = P.count;
-  const int x0 = blockIdx.x * 32, y0 = blockIdx.y * ROWS, z0 = blockIdx.z * VPT;
+  const int x0 = blockIdx.x * 32, y0 = blockIdx.y * ROWS, z0 = P.zBegin + blockIdx.z * VPT;
   const int tid = threadIdx.y * 32 + threadIdx.x;
   const uint32_t full0 = smemAddr(&bars[0]);
   const uint32_t empty0 = smemAddr(&bars[NS]);
@@ -323,11 +323,13 @@ __global__ void __launch_bounds__(32 * (ROWS + 1), LOLA_STAGED_MIN_BLOCKS)
   const int x = x0 + threadIdx.x, y = y0 + threadIdx.y;
   const bool inXY = (x < N) && (y < N);
   const size_t slice = (size_t)N * (size_t)N;
-  float *vcol = a.volume + ((size_t)z0 * N + (size_t)(inXY ? y : 0)) * (size_t)N + (inXY ? x : 0);
+  /* the plan holds only the slab z in [zBegin, zEnd) */
+  float *vcol = a.volume + ((size_t)(z0 - P.zBegin) * N + (size_t)(inXY ? y : 0)) * (size_t)N +
+                (inXY ? x : 0);
   float acc[VPT], comp[VPT];
 #pragma unroll
   for (int k = 0; k < VPT; ++k) {
-    acc[k] = (inXY && z0 + k < N) ? vcol[k * slice] : 0.0f;
+    acc[k] = (inXY && z0 + k < P.zEnd) ? vcol[k * slice] : 0.0f;
     comp[k] = 0.0f;
   }
   const float fi = (float)threadIdx.x, fj = (float)threadIdx.y;
@@ -360,7 +362,7 @@ __global__ void __launch_bounds__(32 * (ROWS + 1), LOLA_STAGED_MIN_BLOCKS)
   }
 #pragma unroll
   for (int k = 0; k < VPT; ++k) {
-    if (inXY && z0 + k < N)
+    if (inXY && z0 + k < P.zEnd)
       vcol[k * slice] = KAHAN ? (acc[k] - comp[k]) : acc[k];
   }
 }
@@ -371,7 +373,8 @@ int launchStagedShape(const PassArgs &a, const LolaPassParams *P, const StageArg
 {
   const int N = P->N;
   const dim3 block(32, ROWS + 1);
-  const dim3 grid((N + 31) / 32, (N + ROWS - 1) / ROWS, (N + VPT - 1) / VPT);
+  const int nz = P->zEnd - P->zBegin;
+  const dim3 grid((N + 31) / 32, (N + ROWS - 1) / ROWS, (nz + VPT - 1) / VPT);
   const size_t smem = (size_t)LOLA_STAGES * (size_t)g.stageBytes;
   auto kernel = stagedPassKernel<S, VPT, ROWS, KAHAN>;
   cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,

@@ -297,7 +297,7 @@ static int planInit(LolaCudaPlan *p)
   s->slotElems = (px + 255) & ~(size_t)255;  /* slot bases 512 B aligned */
   p->imageElems = (size_t)g->imageWidth * (size_t)g->imageHeight;
 
-  const size_t nvox = (size_t)g->problemSize * g->problemSize * g->problemSize;
+  const size_t nvox = lolaPlanVoxels(p);
   CUDA_TRY(cudaMalloc((void **)&p->d_volume, nvox * sizeof(float)));
   CUDA_TRY(cudaMemsetAsync(p->d_volume, 0, nvox * sizeof(float), p->stream));
   CUDA_TRY(cudaMalloc(&p->d_ring, (size_t)p->cfg.batch * s->slotElems * s->elemBytes));
@@ -361,6 +361,14 @@ int lolaCudaPlanCreate(const LolaCudaGeometry *g, const LolaCudaConfig *cfg, Lol
   if (p == NULL)
     return setError("out of host memory");
   p->geom = *g;
+  if (p->geom.sliceCount == 0 && p->geom.sliceBegin == 0)
+    p->geom.sliceCount = g->problemSize;
+  if (p->geom.sliceBegin < 0 || p->geom.sliceCount <= 0 ||
+      p->geom.sliceBegin + p->geom.sliceCount > g->problemSize) {
+    free(p);
+    return setError("slab [%d, %d) outside the %d slices", g->sliceBegin,
+        g->sliceBegin + g->sliceCount, g->problemSize);
+  }
   p->cfg = c;
   p->device = c.device;
   if (!planInit(p)) {
@@ -383,10 +391,29 @@ void *lolaCudaPlanStream(LolaCudaPlan *p)
   return p ? (void *)p->stream : NULL;
 }
 
-static size_t volumeBytes(const LolaCudaPlan *p)
+size_t lolaPlanVoxels(const LolaCudaPlan *p)
 {
   const size_t n = (size_t)p->geom.problemSize;
-  return n * n * n * sizeof(float);
+  return n * n * (size_t)p->geom.sliceCount;
+}
+
+static size_t volumeBytes(const LolaCudaPlan *p)
+{
+  return lolaPlanVoxels(p) * sizeof(float);
+}
+
+int lolaCudaSlab(int N, int rank, int ranks, int align, int32_t *begin, int32_t *count)
+{
+  if (N <= 0 || ranks <= 0 || rank < 0 || rank >= ranks || align <= 0 || begin == NULL ||
+      count == NULL)
+    return setError("slab: invalid arguments");
+  const int units = (N + align - 1) / align;
+  const int b = (int)((long long)units * rank / ranks) * align;
+  int e = (int)((long long)units * (rank + 1) / ranks) * align;
+  e = e > N ? N : e;
+  *begin = b;
+  *count = e > b ? e - b : 0;
+  return 1;
 }
 
 int lolaCudaPlanZeroVolume(LolaCudaPlan *p)
@@ -628,6 +655,8 @@ static int launchPass(LolaCudaPlan *p, const double *mats, int count)
   memset(&P, 0, sizeof(P));
   P.N = p->geom.problemSize;
   P.count = count;
+  P.zBegin = p->geom.sliceBegin;
+  P.zEnd = p->geom.sliceBegin + p->geom.sliceCount;
   P.voxelSize = p->geom.voxelSize;
   P.originIndex = p->geom.originIndex;
   P.accumulation = p->cfg.accumulation;
@@ -875,6 +904,8 @@ int lolaCudaPrepare(RabbitCtGlobalData *d)
   g.imageHeight = (int32_t)d->imageHeight;
   g.voxelSize = d->voxelSize;
   g.originIndex = d->O_Index;
+  g.sliceBegin = 0;
+  g.sliceCount = 0;
   if (d->volumeData == NULL) {
     setError("volumeData is null");
     return moduleFail("prepare");

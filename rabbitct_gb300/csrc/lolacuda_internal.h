@@ -46,6 +46,8 @@ typedef struct {
 typedef struct {
   int32_t N;
   int32_t count;        /* projections in this pass, 1..LOLA_MAX_BATCH */
+  int32_t zBegin;       /* slab of the volume held by this pass: z in [zBegin, zEnd) */
+  int32_t zEnd;
   float voxelSize;
   float originIndex;
   int32_t accumulation; /* LOLA_ACCUM_* */
@@ -81,6 +83,9 @@ int lolaLaunchPack(const LolaStoreDesc *store, const float *d_src, size_t srcStr
 int lolaLaunchBackproject(const LolaStoreDesc *store, const LolaPassParams *params,
     const LolaStageDesc *stage, const void *d_ring, float *d_volume,
     unsigned long long *d_tileCounters, void *stream);
+
+/* Voxels of a plan's volume (N^3). */
+size_t lolaPlanVoxels(const LolaCudaPlan *plan);
 
 /* Sets the thread's lolaCudaLastError() message; returns 0. */
 int lolaSetError(const char *fmt, ...);

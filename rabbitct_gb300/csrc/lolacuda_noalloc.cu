@@ -146,6 +146,8 @@ extern "C" int lolaCudaBackprojectNoAlloc(const LolaCudaGeometry *g, const LolaC
       return lolaSetError("pack launch failed: %s", cudaGetErrorString((cudaError_t)rc));
     P.N = g->problemSize;
     P.count = n;
+    P.zBegin = 0;
+    P.zEnd = g->problemSize;
     P.voxelSize = g->voxelSize;
     P.originIndex = g->originIndex;
     P.accumulation = c.accumulation;

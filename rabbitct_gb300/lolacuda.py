@@ -13,7 +13,14 @@ from . import _native
 from ._native import (LolaCudaConfig, LolaCudaGeometry, LolaCudaStats, Projection,
                       RabbitCtGlobalData, check, config, load_lolacuda)
 
-__all__ = ["Plan", "DeviceBuffer", "GlobalData", "module_functions", "config"]
+__all__ = ["Plan", "DeviceBuffer", "GlobalData", "module_functions", "config", "slab"]
+
+
+def slab(n: int, rank: int, ranks: int, align: int = 8) -> tuple[int, int]:
+    """(sliceBegin, sliceCount) of `rank` among `ranks` (lolaCudaSlab)."""
+    b, c = C.c_int32(), C.c_int32()
+    check(load_lolacuda().lolaCudaSlab(n, rank, ranks, align, C.byref(b), C.byref(c)), "slab")
+    return b.value, c.value
 
 
 class DeviceBuffer:
@@ -55,10 +62,13 @@ class Plan:
     """One reconstruction volume on the device plus its projection ring."""
 
     def __init__(self, n: int, voxel_size: float, origin_index: float, width: int, height: int,
-                 cfg: LolaCudaConfig | None = None, **cfg_kw):
+                 cfg: LolaCudaConfig | None = None, slab: tuple[int, int] | None = None,
+                 **cfg_kw):
         self.lib = load_lolacuda()
         self.n, self.width, self.height = int(n), int(width), int(height)
-        g = LolaCudaGeometry(self.n, self.width, self.height, voxel_size, origin_index)
+        self.slab = (0, self.n) if slab is None else (int(slab[0]), int(slab[1]))
+        g = LolaCudaGeometry(self.n, self.width, self.height, voxel_size, origin_index,
+                             self.slab[0], self.slab[1])
         self.cfg = cfg if cfg is not None else config(**cfg_kw)
         h = C.c_void_p()
         check(self.lib.lolaCudaPlanCreate(C.byref(g), C.byref(self.cfg), C.byref(h)),
@@ -78,12 +88,13 @@ class Plan:
 
     def upload(self, vol: np.ndarray) -> None:
         vol = np.ascontiguousarray(vol, np.float32)
-        assert vol.size == self.n ** 3
+        assert vol.size == self.n * self.n * self.slab[1]
         check(self.lib.lolaCudaPlanUploadVolume(self.handle, vol.ctypes.data), "upload volume")
 
     def download(self, out: np.ndarray | None = None) -> np.ndarray:
+        """The plan's volume (its slab: sliceCount x N x N), z slowest."""
         if out is None:
-            out = np.empty((self.n, self.n, self.n), np.float32)
+            out = np.empty((self.slab[1], self.n, self.n), np.float32)
         check(self.lib.lolaCudaPlanDownloadVolume(self.handle, out.ctypes.data), "download")
         return out
 
@@ -113,6 +124,18 @@ class Plan:
         ms = C.c_double()
         check(self.lib.lolaCudaPlanTimerStop(self.handle, C.byref(ms)), "timer stop")
         return ms.value
+
+    def verify(self, reference_hu: np.ndarray, hus, convert_in_place: bool = False) -> dict:
+        """The runner's -c verification on the device (see lolaCudaPlanVerify)."""
+        from ._native import LolaCudaQuality
+        ref = np.ascontiguousarray(reference_hu, np.uint16)
+        assert ref.size == self.n * self.n * self.slab[1]
+        h = np.asarray(hus, np.float32)
+        q = LolaCudaQuality()
+        check(self.lib.lolaCudaPlanVerify(self.handle, ref.ctypes.data, h.ctypes.data,
+                                          int(convert_in_place), C.byref(q)), "verify")
+        return {"rmse_hu": q.rmse, "mse_hu2": q.mse, "max_abs_hu": q.maxAbs,
+                "psnr_db": q.psnr, "histogram": list(q.histogram)}
 
     def stats(self) -> LolaCudaStats:
         s = LolaCudaStats()
