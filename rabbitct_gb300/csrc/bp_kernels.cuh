@@ -252,13 +252,9 @@ __device__ __forceinline__ void texTaps(unsigned long long tex, float cx, float 
 
 /* Mixed layouts: the 2x2 quads of the F16Q / F32Q layouts, also bound as an
  * RGBA texture (one texel = one quad).  Voxels whose bit is set in
- * LOLA_MIXED_TEX_MASK (default: 2 of every 8, the best split measured on
- * GB300) fetch their quad through the texture unit (a point fetch, widened
- * to FP32 there), the others through the load path, so both gather pipes
- * work in parallel. */
-#ifndef LOLA_MIXED_TEX_MASK
-#define LOLA_MIXED_TEX_MASK 0x8888u
-#endif
+ * LOLA_MIXED_TEX_MASK (lolacuda_internal.h) fetch their quad through the
+ * texture unit (a point fetch, widened to FP32 there), the others through the
+ * load path, so both gather pipes work in parallel. */
 
 template <> struct Layout<LOLA_STORE_F16QX> : Layout<LOLA_STORE_F16Q> {
   static constexpr bool kMixed = true;

@@ -57,6 +57,12 @@ typedef struct {
   LolaPassProj proj[LOLA_MAX_BATCH];
 } LolaPassParams;
 
+/* Mixed layouts: voxels (bit k of each 8, per thread) that fetch through the
+ * texture unit; 2 of every 8 measured best on GB300. */
+#ifndef LOLA_MIXED_TEX_MASK
+#define LOLA_MIXED_TEX_MASK 0x8888u
+#endif
+
 /* Stage buffers of the staged pass (a build-time tuning knob). */
 #ifndef LOLA_STAGES
 #define LOLA_STAGES 3

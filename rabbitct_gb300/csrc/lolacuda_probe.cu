@@ -17,6 +17,7 @@
 #include <stdint.h>
 
 #include "lolaCuda.h"
+#include "lolacuda_internal.h"
 
 namespace {
 
@@ -43,7 +44,7 @@ __global__ void __launch_bounds__(256) issueProbe(float *out, int iters, float a
 }
 
 /* kind: 0 = 4 x FP32 taps, 1 = 4 x 16-bit taps, 2 = 1 x 16 B quad, 3 = 1 x 8 B quad,
- * 4 = one 4-texel texture gather (tld4) */
+ * 4 = one 4-texel texture gather (tld4), 5 = one point fetch of an RGBA texel */
 template <int KIND>
 __global__ void __launch_bounds__(256) gatherProbe(const void *img, int pitch, int rows,
     int iters, float *out, cudaTextureObject_t tex)
@@ -71,10 +72,15 @@ __global__ void __launch_bounds__(256) gatherProbe(const void *img, int pitch, i
     } else if (KIND == 3) {
       const uint2 q = __ldg(static_cast<const uint2 *>(img) + idx);
       acc += __uint_as_float(q.x) + __uint_as_float(q.y);
-    } else {
+    } else if (KIND == 4) {
       const float cx = (float)(idx % (uint32_t)pitch) + 1.0f;
       const float cy = (float)(idx / (uint32_t)pitch) + 1.0f;
       const float4 g = tex2Dgather<float4>(tex, cx, cy, 0);
+      acc += (g.x + g.y) + (g.z + g.w);
+    } else {
+      const float cx = (float)(idx % (uint32_t)pitch) + 0.5f;
+      const float cy = (float)(idx / (uint32_t)pitch) + 0.5f;
+      const float4 g = tex2D<float4>(tex, cx, cy);
       acc += (g.x + g.y) + (g.z + g.w);
     }
   }
@@ -121,9 +127,25 @@ extern "C" double lolaCudaProbeIssueRate(void)
 
 /* Voxel updates per second the gather alone sustains, for a storage layout
  * (LOLA_STORE_*) over a width x height detector padded like the pass kernel. */
+static double probeKind(int kind, int elem, int channels, int width, int height);
+
 extern "C" double lolaCudaProbeGatherRate(int storage, int width, int height)
 {
-  const int pitch = (width + 128 + 31) & ~31, rows = height + 128;
+  if (storage == LOLA_STORE_F16QX || storage == LOLA_STORE_F32QX) {
+    /* the two pipes run in parallel on their shares of the voxels */
+    const int elem = storage == LOLA_STORE_F16QX ? 8 : 16;
+    const double lsu = probeKind(elem == 8 ? 3 : 2, elem, 1, width, height);
+    const double tex = probeKind(5, elem, 4, width, height);
+    const double ft = __builtin_popcount(LOLA_MIXED_TEX_MASK & 0xFFu) / 8.0;
+    if (lsu <= 0.0 || tex <= 0.0)
+      return -1.0;
+    if (ft <= 0.0)
+      return lsu;
+    if (ft >= 1.0)
+      return tex;
+    const double a = lsu / (1.0 - ft), b = tex / ft;
+    return a < b ? a : b;
+  }
   int kind, elem;
   switch (storage) {
   case LOLA_STORE_F32: kind = 0; elem = 4; break;
@@ -136,6 +158,12 @@ extern "C" double lolaCudaProbeGatherRate(int storage, int width, int height)
   case LOLA_STORE_TEX16: kind = 4; elem = 2; break;
   default: return -1.0;
   }
+  return probeKind(kind, elem, 1, width, height);
+}
+
+static double probeKind(int kind, int elem, int channels, int width, int height)
+{
+  const int pitch = (width + 128 + 31) & ~31, rows = height + 128;
   const size_t bytes = (size_t)pitch * rows * elem;
   void *img = nullptr;
   float *out = nullptr;
@@ -147,11 +175,13 @@ extern "C" double lolaCudaProbeGatherRate(int storage, int width, int height)
   }
   cudaMemset(img, 0, bytes);
   cudaTextureObject_t tex = 0;
-  if (kind == 4) {
+  if (kind >= 4) {
     cudaResourceDesc rd = {};
     rd.resType = cudaResourceTypePitch2D;
     rd.res.pitch2D.devPtr = img;
-    rd.res.pitch2D.desc = cudaCreateChannelDesc(8 * elem, 0, 0, 0, cudaChannelFormatKindFloat);
+    const int bits = 8 * elem / channels;
+    rd.res.pitch2D.desc = cudaCreateChannelDesc(bits, channels > 1 ? bits : 0,
+        channels > 1 ? bits : 0, channels > 1 ? bits : 0, cudaChannelFormatKindFloat);
     rd.res.pitch2D.width = (size_t)pitch;
     rd.res.pitch2D.height = (size_t)rows;
     rd.res.pitch2D.pitchInBytes = (size_t)pitch * elem;
@@ -176,7 +206,8 @@ extern "C" double lolaCudaProbeGatherRate(int storage, int width, int height)
     case 1: gatherProbe<1><<<blocks, threads>>>(img, pitch, rows, it, out, tex); break;
     case 2: gatherProbe<2><<<blocks, threads>>>(img, pitch, rows, it, out, tex); break;
     case 3: gatherProbe<3><<<blocks, threads>>>(img, pitch, rows, it, out, tex); break;
-    default: gatherProbe<4><<<blocks, threads>>>(img, pitch, rows, it, out, tex); break;
+    case 4: gatherProbe<4><<<blocks, threads>>>(img, pitch, rows, it, out, tex); break;
+    default: gatherProbe<5><<<blocks, threads>>>(img, pitch, rows, it, out, tex); break;
     }
   };
   launch(64);
