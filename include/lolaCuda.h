@@ -200,6 +200,43 @@ int lolaCudaPlanTimerStop(LolaCudaPlan *plan, double *ms);
 int lolaCudaPlanGetStats(LolaCudaPlan *plan, LolaCudaStats *stats);
 int lolaCudaPlanResetStats(LolaCudaPlan *plan);
 
+/* ---- Batched reconstructions ---------------------------------------------------
+ * No counterpart in the reference, whose runner drives one reconstruction per
+ * process.  Many volumes of uneven size, detector and projection count are
+ * reconstructed together: waves of `batch` projections of every job, each
+ * wave one pack launch and one persistent pass launch whose blocks pull
+ * (job, tile) work items from a counter, the whole run captured into a CUDA
+ * graph at create and replayed by each run.  All jobs share the config's
+ * storage, accumulation and batch; FP32 arithmetic throughout. */
+typedef struct {
+  LolaCudaGeometry geometry;   /* whole volume: slice fields must be 0 */
+  int32_t projections;
+  int32_t reserved;
+  const float *d_images;       /* projections x imageHeight x imageWidth FP32, device */
+  const double *h_matrices;    /* projections x 12, host; copied at create */
+  float *d_volume;             /* N^3 FP32, device, caller-owned; accumulated into */
+} LolaCudaJob;
+
+typedef struct {
+  int32_t jobs;
+  int32_t waves;
+  int32_t blocks;              /* persistent blocks per pass launch */
+  int32_t launchesPerRun;
+  double voxelUpdates;         /* sum over jobs of N^3 x projections */
+  size_t ringBytes;
+} LolaCudaBatchInfo;
+
+typedef struct LolaCudaBatch LolaCudaBatch;
+
+int lolaCudaBatchCreate(const LolaCudaJob *jobs, int njobs, const LolaCudaConfig *config,
+    LolaCudaBatch **batch);
+/* Replays the captured run on the batch's stream (asynchronous). */
+int lolaCudaBatchRun(LolaCudaBatch *batch);
+int lolaCudaBatchSynchronize(LolaCudaBatch *batch);
+void *lolaCudaBatchStream(LolaCudaBatch *batch);
+int lolaCudaBatchGetInfo(LolaCudaBatch *batch, LolaCudaBatchInfo *info);
+int lolaCudaBatchDestroy(LolaCudaBatch *batch);
+
 /* ---- Verification on the device ------------------------------------------------
  * The runner's -c check (src/rabbitRunner.c:320-384) without copying the
  * volume to the host: HU = floor(hus[0] * v + hus[1] + 0.5) for v > 0 else 0,

@@ -67,6 +67,18 @@ class LolaCudaQuality(C.Structure):
                 ("psnr", C.c_double), ("histogram", C.c_uint64 * 11)]
 
 
+class LolaCudaJob(C.Structure):
+    _fields_ = [("geometry", LolaCudaGeometry), ("projections", C.c_int32),
+                ("reserved", C.c_int32), ("d_images", C.c_void_p),
+                ("h_matrices", C.c_void_p), ("d_volume", C.c_void_p)]
+
+
+class LolaCudaBatchInfo(C.Structure):
+    _fields_ = [("jobs", C.c_int32), ("waves", C.c_int32), ("blocks", C.c_int32),
+                ("launchesPerRun", C.c_int32), ("voxelUpdates", C.c_double),
+                ("ringBytes", C.c_size_t)]
+
+
 class LolaCudaStats(C.Structure):
     _fields_ = [("passes", C.c_int64),
                 ("packs", C.c_int64),
@@ -125,6 +137,12 @@ _SIGNATURES = [
     ("lolaCudaPlanVerify", C.c_int, [_P, _P, _P, C.c_int, C.POINTER(LolaCudaQuality)]),
     ("lolaCudaSlab", C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int32),
                                C.POINTER(C.c_int32)]),
+    ("lolaCudaBatchCreate", C.c_int, [_P, C.c_int, C.POINTER(LolaCudaConfig), C.POINTER(_P)]),
+    ("lolaCudaBatchRun", C.c_int, [_P]),
+    ("lolaCudaBatchSynchronize", C.c_int, [_P]),
+    ("lolaCudaBatchStream", _P, [_P]),
+    ("lolaCudaBatchGetInfo", C.c_int, [_P, C.POINTER(LolaCudaBatchInfo)]),
+    ("lolaCudaBatchDestroy", C.c_int, [_P]),
     ("lolaCudaHostAlloc", _P, [C.c_size_t]),
     ("lolaCudaHostFree", C.c_int, [_P]),
     ("lolaCudaProbeIssueRate", C.c_double, []),

@@ -27,7 +27,7 @@ CU_SOURCES = [
     "bp_f32.cu", "bp_f16.cu", "bp_bf16.cu", "bp_f32q.cu", "bp_f16q.cu", "bp_bf16q.cu",
     "bp_tex32.cu", "bp_tex16.cu", "bp_f16qx.cu", "bp_f32qx.cu",
     "lolacuda_dispatch.cu", "lolacuda_probe.cu", "lolacuda_noalloc.cu",
-    "lolacuda_geometry.cu", "lolacuda_verify.cu",
+    "lolacuda_geometry.cu", "lolacuda_verify.cu", "lolacuda_batch.cu",
 ]
 C_SOURCES = ["lolacuda_host.c"]
 
@@ -72,7 +72,8 @@ def build_lolacuda(force: bool = False, jobs: int | None = None) -> Path:
     cuda = _cuda_home()
     nvcc = str(cuda / "bin" / "nvcc")
     out = LIB / "liblolacuda.so"
-    headers = [CSRC / "bp_kernels.cuh", CSRC / "bp_staged.cuh", CSRC / "lolacuda_internal.h",
+    headers = [CSRC / "bp_kernels.cuh", CSRC / "bp_staged.cuh", CSRC / "bp_batch.cuh",
+               CSRC / "lolacuda_internal.h",
                INCLUDE / "lolaCuda.h"]
     common_inc = ["-I" + str(INCLUDE), "-I" + str(CSRC)]
 

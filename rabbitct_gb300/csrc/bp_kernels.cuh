@@ -389,17 +389,24 @@ __device__ __forceinline__ void applyProjection(const TileProj &tp, const void *
  * origin (phase A, one thread per projection) and the footprint and mode from
  * the 8 tile corners (phase B, 8 lanes per projection).  Ends with the block
  * synchronised and sp[0 .. count) complete.  nthreads is a multiple of 32. */
+/* Geometry of one volume and its stored projections, as setupTile needs it. */
+struct TileGeom {
+  int N;          /* volume edge */
+  int zEnd;       /* end of the slab held */
+  float voxelSize, originIndex;
+  int width, height, margin;
+};
+
 template <int ROWS, int VPT>
-__device__ __forceinline__ void setupTile(const LolaPassParams &P, const PassArgs &a,
-    TileProj *sp, int tid, int nthreads, int x0, int y0, int z0)
+__device__ __forceinline__ void setupTileGeom(const LolaPassProj *proj, int count,
+    const TileGeom &g, TileProj *sp, int tid, int nthreads, int x0, int y0, int z0)
 {
-  const int N = P.N;
-  const int count = P.count;
+  const int N = g.N;
   /* -- setup A: FP64 projection of the tile origin, one thread per view -- */
   if (tid < count) {
-    const LolaPassProj &pp = P.proj[tid];
+    const LolaPassProj &pp = proj[tid];
     const double *m = pp.a;
-    const double vs = (double)P.voxelSize, o = (double)P.originIndex;
+    const double vs = (double)g.voxelSize, o = (double)g.originIndex;
     const double X = o + (double)x0 * vs, Y = o + (double)y0 * vs, Z = o + (double)z0 * vs;
     const double U = m[0] * X + m[3] * Y + m[6] * Z + m[9];
     const double V = m[1] * X + m[4] * Y + m[7] * Z + m[10];
@@ -426,7 +433,7 @@ __device__ __forceinline__ void setupTile(const LolaPassParams &P, const PassArg
 
   /* -- setup B: footprint of the tile from its 8 corners, 8 lanes per view -- */
   const int ex = min(32, N - x0) - 1, ey = min(ROWS, N - y0) - 1;
-  const int ez = min(VPT, P.zEnd - z0) - 1;
+  const int ez = min(VPT, g.zEnd - z0) - 1;
   for (int base = 0; base < 8 * count; base += nthreads) {
     const int t = base + tid;
     const bool active = t < 8 * count;
@@ -452,7 +459,7 @@ __device__ __forceinline__ void setupTile(const LolaPassParams &P, const PassArg
     }
     if (active && c == 0) {
       const float slack = 0.5f;
-      const float W = (float)a.width, H = (float)a.height, M = (float)a.margin;
+      const float W = (float)g.width, H = (float)g.height, M = (float)g.margin;
       int mode;
       if (!ok)
         mode = MODE_SLOW;
@@ -473,6 +480,21 @@ __device__ __forceinline__ void setupTile(const LolaPassParams &P, const PassArg
   }
   __syncthreads();
 
+}
+
+template <int ROWS, int VPT>
+__device__ __forceinline__ void setupTile(const LolaPassParams &P, const PassArgs &a,
+    TileProj *sp, int tid, int nthreads, int x0, int y0, int z0)
+{
+  TileGeom g;
+  g.N = P.N;
+  g.zEnd = P.zEnd;
+  g.voxelSize = P.voxelSize;
+  g.originIndex = P.originIndex;
+  g.width = a.width;
+  g.height = a.height;
+  g.margin = a.margin;
+  setupTileGeom<ROWS, VPT>(P.proj, P.count, g, sp, tid, nthreads, x0, y0, z0);
 }
 
 /* Resident blocks per SM requested from the register allocator.  The pass is
@@ -641,4 +663,17 @@ int launchPass(const LolaStoreDesc *st, const LolaPassParams *P, const void *rin
           static_cast<cudaStream_t>(stream));                                              \
     return lola::launchPass<S>(st, P, ring, volume, counters,                              \
         static_cast<cudaStream_t>(stream));                                                \
+  }                                                                                        \
+  extern "C" int lolaLaunchBatchPack_##NAME(const LolaBatchWave *w, void *stream)          \
+  {                                                                                        \
+    return lola::launchBatchPack<S>(w, static_cast<cudaStream_t>(stream));                 \
+  }                                                                                        \
+  extern "C" int lolaLaunchBatchPass_##NAME(const LolaBatchWave *w, int blocks,            \
+      void *stream)                                                                        \
+  {                                                                                        \
+    return lola::launchBatchPass<S>(w, blocks, static_cast<cudaStream_t>(stream));         \
+  }                                                                                        \
+  extern "C" int lolaBatchOccupancy_##NAME(int accumulation, int *blocks)                  \
+  {                                                                                        \
+    return lola::batchOccupancy<S>(accumulation, blocks);                                  \
   }

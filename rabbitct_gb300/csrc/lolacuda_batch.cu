@@ -1,0 +1,337 @@
+/* Batched reconstructions: many volumes of uneven size, detector and
+ * projection count, reconstructed together (host side of bp_batch.cuh).
+ *
+ * lolaCudaBatchCreate lays out one projection ring holding `b` stored slots
+ * per job, the per-wave projection parameters of every job, and per-wave
+ * work lists (prefix sums of the tiles of the jobs that still have
+ * projections in that wave), then captures the whole run — a counter reset,
+ * and per wave one pack launch and one persistent pass launch — into a CUDA
+ * graph.  lolaCudaBatchRun replays the graph on the batch's stream.
+ */
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "lolaCuda.h"
+#include "lolacuda_internal.h"
+
+struct LolaCudaBatch {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  LolaCudaConfig cfg;
+  int njobs = 0, b = 0, waves = 0, blocks = 0, launches = 0;
+  double updates = 0.0;
+  size_t ringBytes = 0;
+  unsigned char *d_ring = nullptr;
+  LolaBatchJob *d_jobs = nullptr;
+  long long *d_prefix = nullptr;
+  LolaPassProj *d_proj = nullptr;
+  int *d_counters = nullptr;
+  unsigned long long *d_tex = nullptr;
+  std::vector<cudaTextureObject_t> textures;
+};
+
+namespace {
+
+int pixelBytes(int storage)
+{
+  switch (storage) {
+  case LOLA_STORE_F32: case LOLA_STORE_TEX32: return 4;
+  case LOLA_STORE_F16: case LOLA_STORE_BF16: case LOLA_STORE_TEX16: return 2;
+  case LOLA_STORE_F32Q: case LOLA_STORE_F32QX: return 16;
+  case LOLA_STORE_F16Q: case LOLA_STORE_BF16Q: case LOLA_STORE_F16QX: return 8;
+  default: return 0;
+  }
+}
+
+int textureChannels(int storage)
+{
+  switch (storage) {
+  case LOLA_STORE_TEX32: case LOLA_STORE_TEX16: return 1;
+  case LOLA_STORE_F16QX: case LOLA_STORE_F32QX: return 4;
+  default: return 0;
+  }
+}
+
+void release(LolaCudaBatch *bt)
+{
+  if (bt == nullptr)
+    return;
+  cudaSetDevice(bt->device);
+  if (bt->stream)
+    cudaStreamSynchronize(bt->stream);
+  if (bt->exec)
+    cudaGraphExecDestroy(bt->exec);
+  if (bt->graph)
+    cudaGraphDestroy(bt->graph);
+  for (cudaTextureObject_t t : bt->textures)
+    cudaDestroyTextureObject(t);
+  cudaFree(bt->d_ring);
+  cudaFree(bt->d_jobs);
+  cudaFree(bt->d_prefix);
+  cudaFree(bt->d_proj);
+  cudaFree(bt->d_counters);
+  cudaFree(bt->d_tex);
+  if (bt->stream)
+    cudaStreamDestroy(bt->stream);
+  delete bt;
+}
+
+#define BT_TRY(call)                                                                      \
+  do {                                                                                    \
+    cudaError_t e_ = (call);                                                              \
+    if (e_ != cudaSuccess) {                                                              \
+      lolaSetError("batch: %s: %s", #call, cudaGetErrorString(e_));                       \
+      return 0;                                                                           \
+    }                                                                                     \
+  } while (0)
+
+int build(LolaCudaBatch *bt, const LolaCudaJob *jobs)
+{
+  const int nj = bt->njobs, b = bt->b, storage = bt->cfg.storage;
+  const int pix = pixelBytes(storage);
+  BT_TRY(cudaSetDevice(bt->device));
+  BT_TRY(cudaStreamCreateWithFlags(&bt->stream, cudaStreamNonBlocking));
+
+  /* per-job stored layouts and the shared ring */
+  std::vector<LolaBatchJob> hj(nj);
+  std::vector<size_t> ringOffset(nj);
+  int maxPitch = 0, maxRows = 0;
+  size_t ring = 0;
+  for (int j = 0; j < nj; ++j) {
+    const LolaCudaGeometry &g = jobs[j].geometry;
+    LolaBatchJob &J = hj[j];
+    memset(&J, 0, sizeof(J));
+    J.N = g.problemSize;
+    J.width = g.imageWidth;
+    J.height = g.imageHeight;
+    J.margin = LOLA_MARGIN;
+    J.pitch = (g.imageWidth + 2 * LOLA_MARGIN + 31) & ~31;
+    J.rows = g.imageHeight + 2 * LOLA_MARGIN;
+    if ((long long)J.pitch * J.rows >= (1LL << 23) - 2 * (long long)J.pitch)
+      return lolaSetError("batch: job %d detector %dx%d too large", j, g.imageWidth,
+          g.imageHeight);
+    J.slotElems = ((size_t)J.pitch * J.rows + 255) & ~(size_t)255;
+    J.slotBytes = J.slotElems * pix;
+    J.voxelSize = g.voxelSize;
+    J.originIndex = g.originIndex;
+    J.tilesX = (J.N + 31) / 32;
+    J.tilesY = (J.N + 7) / 8;
+    J.tilesZ = (J.N + 7) / 8;
+    J.nproj = jobs[j].projections;
+    J.volume = jobs[j].d_volume;
+    J.images = jobs[j].d_images;
+    ringOffset[j] = ring;
+    ring += (size_t)b * J.slotBytes;
+    maxPitch = J.pitch > maxPitch ? J.pitch : maxPitch;
+    maxRows = J.rows > maxRows ? J.rows : maxRows;
+    bt->updates += (double)J.N * J.N * J.N * J.nproj;
+    const int w = (J.nproj + b - 1) / b;
+    bt->waves = w > bt->waves ? w : bt->waves;
+  }
+  bt->ringBytes = ring;
+  BT_TRY(cudaMalloc(&bt->d_ring, ring));
+  BT_TRY(cudaMemset(bt->d_ring, 0, ring));
+
+  const int ch = textureChannels(storage);
+  std::vector<unsigned long long> texHandles;
+  if (ch > 0) {
+    texHandles.resize((size_t)nj * b);
+    for (int j = 0; j < nj; ++j)
+      for (int s = 0; s < b; ++s) {
+        cudaResourceDesc rd;
+        memset(&rd, 0, sizeof(rd));
+        rd.resType = cudaResourceTypePitch2D;
+        rd.res.pitch2D.devPtr = bt->d_ring + ringOffset[j] + (size_t)s * hj[j].slotBytes;
+        const int bits = 8 * pix / ch;
+        rd.res.pitch2D.desc = cudaCreateChannelDesc(bits, ch > 1 ? bits : 0, ch > 1 ? bits : 0,
+            ch > 1 ? bits : 0, cudaChannelFormatKindFloat);
+        rd.res.pitch2D.width = (size_t)hj[j].pitch;
+        rd.res.pitch2D.height = (size_t)hj[j].rows;
+        rd.res.pitch2D.pitchInBytes = (size_t)hj[j].pitch * pix;
+        cudaTextureDesc td;
+        memset(&td, 0, sizeof(td));
+        td.addressMode[0] = cudaAddressModeBorder;
+        td.addressMode[1] = cudaAddressModeBorder;
+        td.filterMode = cudaFilterModePoint;
+        td.readMode = cudaReadModeElementType;
+        cudaTextureObject_t t = 0;
+        BT_TRY(cudaCreateTextureObject(&t, &rd, &td, nullptr));
+        bt->textures.push_back(t);
+        texHandles[(size_t)j * b + s] = (unsigned long long)t;
+      }
+    BT_TRY(cudaMalloc(&bt->d_tex, texHandles.size() * sizeof(unsigned long long)));
+    BT_TRY(cudaMemcpy(bt->d_tex, texHandles.data(),
+        texHandles.size() * sizeof(unsigned long long), cudaMemcpyHostToDevice));
+  }
+  for (int j = 0; j < nj; ++j) {
+    hj[j].ring = bt->d_ring + ringOffset[j];
+    hj[j].tex = ch > 0 ? bt->d_tex + (size_t)j * b : nullptr;
+  }
+  BT_TRY(cudaMalloc(&bt->d_jobs, (size_t)nj * sizeof(LolaBatchJob)));
+  BT_TRY(cudaMemcpy(bt->d_jobs, hj.data(), (size_t)nj * sizeof(LolaBatchJob),
+      cudaMemcpyHostToDevice));
+
+  /* per wave: work lists over the jobs still active and their projections */
+  const int W = bt->waves;
+  std::vector<long long> prefix((size_t)W * (nj + 1));
+  std::vector<LolaPassProj> proj((size_t)W * nj * b);
+  memset(proj.data(), 0, proj.size() * sizeof(LolaPassProj));
+  std::vector<long long> totals(W);
+  for (int w = 0; w < W; ++w) {
+    long long acc = 0;
+    for (int j = 0; j < nj; ++j) {
+      prefix[(size_t)w * (nj + 1) + j] = acc;
+      const int count = hj[j].nproj - w * b;
+      if (count > 0)
+        acc += (long long)hj[j].tilesX * hj[j].tilesY * hj[j].tilesZ;
+      for (int s = 0; s < b && s < count; ++s) {
+        const double *m = jobs[j].h_matrices + 12 * (size_t)(w * b + s);
+        LolaPassProj &pp = proj[((size_t)w * nj + j) * b + s];
+        memcpy(pp.a, m, 12 * sizeof(double));
+        for (int ax = 0; ax < 3; ++ax)
+          for (int c = 0; c < 3; ++c)
+            pp.step[ax][c] = (float)(m[ax * 3 + c] * (double)hj[j].voxelSize);
+        pp.slot = s;
+      }
+    }
+    prefix[(size_t)w * (nj + 1) + nj] = acc;
+    totals[w] = acc;
+  }
+  BT_TRY(cudaMalloc(&bt->d_prefix, prefix.size() * sizeof(long long)));
+  BT_TRY(cudaMemcpy(bt->d_prefix, prefix.data(), prefix.size() * sizeof(long long),
+      cudaMemcpyHostToDevice));
+  BT_TRY(cudaMalloc(&bt->d_proj, proj.size() * sizeof(LolaPassProj)));
+  BT_TRY(cudaMemcpy(bt->d_proj, proj.data(), proj.size() * sizeof(LolaPassProj),
+      cudaMemcpyHostToDevice));
+  BT_TRY(cudaMalloc(&bt->d_counters, (size_t)W * sizeof(int)));
+
+  /* persistent grid: every resident slot of the GPU */
+  int sms = 0, perSM = 0;
+  BT_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, bt->device));
+  int rc = lolaBatchPassOccupancy(storage, bt->cfg.accumulation, &perSM);
+  if (rc != 0 || perSM <= 0)
+    return lolaSetError("batch: occupancy query failed (%d)", rc);
+  bt->blocks = sms * perSM;
+
+  /* capture the run */
+  BT_TRY(cudaStreamBeginCapture(bt->stream, cudaStreamCaptureModeThreadLocal));
+  int launchRc = 0;
+  cudaError_t me = cudaMemsetAsync(bt->d_counters, 0, (size_t)W * sizeof(int), bt->stream);
+  for (int w = 0; w < W && me == cudaSuccess && launchRc == 0; ++w) {
+    LolaBatchWave wa;
+    wa.jobs = bt->d_jobs;
+    wa.tilePrefix = bt->d_prefix + (size_t)w * (nj + 1);
+    wa.proj = bt->d_proj + (size_t)w * nj * b;
+    wa.counter = bt->d_counters + w;
+    wa.totalItems = totals[w];
+    wa.njobs = nj;
+    wa.b = b;
+    wa.wave = w;
+    wa.maxPitch = maxPitch;
+    wa.maxRows = maxRows;
+    wa.accumulation = bt->cfg.accumulation;
+    wa.storage = storage;
+    launchRc = lolaLaunchBatchPack(&wa, bt->stream);
+    if (launchRc == 0)
+      launchRc = lolaLaunchBatchPass(&wa, bt->blocks, bt->stream);
+    bt->launches += 2;
+  }
+  cudaError_t ce = cudaStreamEndCapture(bt->stream, &bt->graph);
+  if (me != cudaSuccess || launchRc != 0 || ce != cudaSuccess)
+    return lolaSetError("batch: capture failed: %s / %s / %s", cudaGetErrorString(me),
+        cudaGetErrorString((cudaError_t)launchRc), cudaGetErrorString(ce));
+  BT_TRY(cudaGraphInstantiate(&bt->exec, bt->graph, 0));
+  return 1;
+}
+
+} /* namespace */
+
+extern "C" int lolaCudaBatchCreate(const LolaCudaJob *jobs, int njobs,
+    const LolaCudaConfig *config, LolaCudaBatch **out)
+{
+  if (out == nullptr || jobs == nullptr || njobs <= 0)
+    return lolaSetError("batch: no jobs");
+  *out = nullptr;
+  LolaCudaBatch *bt = new LolaCudaBatch();
+  if (config != nullptr)
+    bt->cfg = *config;
+  else
+    lolaCudaDefaultConfig(&bt->cfg);
+  bt->device = bt->cfg.device;
+  bt->njobs = njobs;
+  bt->b = bt->cfg.batch;
+  if (bt->b < 1 || bt->b > LOLA_MAX_BATCH || pixelBytes(bt->cfg.storage) == 0 ||
+      (bt->cfg.accumulation != LOLA_ACCUM_PLAIN && bt->cfg.accumulation != LOLA_ACCUM_KAHAN)) {
+    delete bt;
+    return lolaSetError("batch: invalid configuration");
+  }
+  for (int j = 0; j < njobs; ++j) {
+    const LolaCudaGeometry &g = jobs[j].geometry;
+    if (g.problemSize <= 0 || g.problemSize > 2048 || g.imageWidth <= 0 ||
+        g.imageHeight <= 0 || !(g.voxelSize > 0.0f) || jobs[j].projections < 0 ||
+        (jobs[j].projections > 0 && (jobs[j].d_images == nullptr ||
+                                     jobs[j].h_matrices == nullptr)) ||
+        jobs[j].d_volume == nullptr) {
+      delete bt;
+      return lolaSetError("batch: job %d is invalid", j);
+    }
+  }
+  if (!build(bt, jobs)) {
+    char msg[512];
+    strncpy(msg, lolaCudaLastError(), sizeof(msg) - 1);
+    msg[sizeof(msg) - 1] = 0;
+    release(bt);
+    return lolaSetError("%s", msg);
+  }
+  *out = bt;
+  return 1;
+}
+
+extern "C" int lolaCudaBatchRun(LolaCudaBatch *bt)
+{
+  if (bt == nullptr)
+    return lolaSetError("batch: null");
+  BT_TRY(cudaSetDevice(bt->device));
+  BT_TRY(cudaGraphLaunch(bt->exec, bt->stream));
+  return 1;
+}
+
+extern "C" int lolaCudaBatchSynchronize(LolaCudaBatch *bt)
+{
+  if (bt == nullptr)
+    return lolaSetError("batch: null");
+  BT_TRY(cudaSetDevice(bt->device));
+  BT_TRY(cudaStreamSynchronize(bt->stream));
+  return 1;
+}
+
+extern "C" void *lolaCudaBatchStream(LolaCudaBatch *bt)
+{
+  return bt ? (void *)bt->stream : nullptr;
+}
+
+extern "C" int lolaCudaBatchGetInfo(LolaCudaBatch *bt, LolaCudaBatchInfo *info)
+{
+  if (bt == nullptr || info == nullptr)
+    return lolaSetError("batch: null argument");
+  info->jobs = bt->njobs;
+  info->waves = bt->waves;
+  info->blocks = bt->blocks;
+  info->launchesPerRun = bt->launches;
+  info->voxelUpdates = bt->updates;
+  info->ringBytes = bt->ringBytes;
+  return 1;
+}
+
+extern "C" int lolaCudaBatchDestroy(LolaCudaBatch *bt)
+{
+  release(bt);
+  return 1;
+}

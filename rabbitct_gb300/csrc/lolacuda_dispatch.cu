@@ -7,7 +7,10 @@
   extern "C" int lolaLaunchPack_##NAME(const LolaStoreDesc *, const float *, size_t,       \
       void *, int, int, void *);                                                           \
   extern "C" int lolaLaunchPass_##NAME(const LolaStoreDesc *, const LolaPassParams *,      \
-      const LolaStageDesc *, const void *, float *, unsigned long long *, void *);
+      const LolaStageDesc *, const void *, float *, unsigned long long *, void *);         \
+  extern "C" int lolaLaunchBatchPack_##NAME(const LolaBatchWave *, void *);                \
+  extern "C" int lolaLaunchBatchPass_##NAME(const LolaBatchWave *, int, void *);           \
+  extern "C" int lolaBatchOccupancy_##NAME(int, int *);
 
 LOLA_DECLARE(F32)
 LOLA_DECLARE(F16)
@@ -70,4 +73,42 @@ extern "C" int lolaKernelShapeSupported(int voxelsPerThread, int rowsPerBlock)
   return (voxelsPerThread == 8 && (rowsPerBlock == 8 || rowsPerBlock == 4)) ||
          (voxelsPerThread == 16 && (rowsPerBlock == 8 || rowsPerBlock == 4)) ||
          (voxelsPerThread == 4 && rowsPerBlock == 8);
+}
+
+#define LOLA_BATCH_CASES(CALL)                                                             \
+  switch (storage) {                                                                       \
+  case LOLA_STORE_F32: return CALL(F32);                                                   \
+  case LOLA_STORE_F16: return CALL(F16);                                                   \
+  case LOLA_STORE_BF16: return CALL(BF16);                                                 \
+  case LOLA_STORE_F32Q: return CALL(F32Q);                                                 \
+  case LOLA_STORE_F16Q: return CALL(F16Q);                                                 \
+  case LOLA_STORE_BF16Q: return CALL(BF16Q);                                               \
+  case LOLA_STORE_TEX32: return CALL(TEX32);                                               \
+  case LOLA_STORE_TEX16: return CALL(TEX16);                                               \
+  case LOLA_STORE_F16QX: return CALL(F16QX);                                               \
+  case LOLA_STORE_F32QX: return CALL(F32QX);                                               \
+  default: return (int)cudaErrorInvalidValue;                                              \
+  }
+
+extern "C" int lolaLaunchBatchPack(const LolaBatchWave *w, void *stream)
+{
+  const int storage = w->storage;
+#define PACK_CALL(NAME) lolaLaunchBatchPack_##NAME(w, stream)
+  LOLA_BATCH_CASES(PACK_CALL)
+#undef PACK_CALL
+}
+
+extern "C" int lolaLaunchBatchPass(const LolaBatchWave *w, int blocks, void *stream)
+{
+  const int storage = w->storage;
+#define PASS_CALL(NAME) lolaLaunchBatchPass_##NAME(w, blocks, stream)
+  LOLA_BATCH_CASES(PASS_CALL)
+#undef PASS_CALL
+}
+
+extern "C" int lolaBatchPassOccupancy(int storage, int accumulation, int *blocks)
+{
+#define OCC_CALL(NAME) lolaBatchOccupancy_##NAME(accumulation, blocks)
+  LOLA_BATCH_CASES(OCC_CALL)
+#undef OCC_CALL
 }

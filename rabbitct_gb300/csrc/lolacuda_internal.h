@@ -80,6 +80,29 @@ typedef struct {
   int *d_error;           /* device flag set on a wait timeout */
 } LolaStageDesc;
 
+/* One reconstruction of a batch (bp_batch.cuh), as the device sees it. */
+typedef struct {
+  float *volume;                    /* N^3 FP32 */
+  const float *images;              /* nproj x height x width FP32 */
+  unsigned char *ring;              /* this job's `b` stored slots */
+  const unsigned long long *tex;    /* device array of b texture objects, or null */
+  size_t slotBytes;
+  size_t slotElems;
+  int32_t N, width, height, margin, pitch, rows;
+  float voxelSize, originIndex;
+  int32_t tilesX, tilesY, tilesZ, nproj;
+} LolaBatchJob;
+
+/* One wave of a batch: projections [wave*b, wave*b + b) of every job. */
+typedef struct {
+  const LolaBatchJob *jobs;         /* device, njobs */
+  const long long *tilePrefix;      /* device, njobs + 1: first work item of each job */
+  const LolaPassProj *proj;         /* device, njobs x b: this wave's projections */
+  int *counter;                     /* device: this wave's work-item counter */
+  long long totalItems;
+  int32_t njobs, b, wave, maxPitch, maxRows, accumulation, storage;
+} LolaBatchWave;
+
 /* Kernel launchers (lolacuda_dispatch.cu).  Return 0 on success or a
  * cudaError_t value. */
 int lolaLaunchPack(const LolaStoreDesc *store, const float *d_src, size_t srcStride,
@@ -95,6 +118,12 @@ size_t lolaPlanVoxels(const LolaCudaPlan *plan);
 
 /* Sets the thread's lolaCudaLastError() message; returns 0. */
 int lolaSetError(const char *fmt, ...);
+
+/* Batched waves: pack every job's slots, then one persistent pass. */
+int lolaLaunchBatchPack(const LolaBatchWave *wave, void *stream);
+int lolaLaunchBatchPass(const LolaBatchWave *wave, int blocks, void *stream);
+/* Resident blocks per SM of the batched pass for a storage layout. */
+int lolaBatchPassOccupancy(int storage, int accumulation, int *blocksPerSM);
 
 /* 1 if the (voxelsPerThread, rowsPerBlock) pair has a compiled kernel. */
 int lolaKernelShapeSupported(int voxelsPerThread, int rowsPerBlock);

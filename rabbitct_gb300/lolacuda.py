@@ -13,7 +13,7 @@ from . import _native
 from ._native import (LolaCudaConfig, LolaCudaGeometry, LolaCudaStats, Projection,
                       RabbitCtGlobalData, check, config, load_lolacuda)
 
-__all__ = ["Plan", "DeviceBuffer", "GlobalData", "module_functions", "config", "slab"]
+__all__ = ["Plan", "Batch", "DeviceBuffer", "GlobalData", "module_functions", "config", "slab"]
 
 
 def slab(n: int, rank: int, ranks: int, align: int = 8) -> tuple[int, int]:
@@ -148,6 +148,63 @@ class Plan:
     def close(self) -> None:
         if getattr(self, "handle", None):
             self.lib.lolaCudaPlanDestroy(self.handle)
+            self.handle = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Batch:
+    """Uneven reconstructions run together (lolaCudaBatchCreate / Run).
+
+    jobs: dicts with keys n, voxel_size, origin_index, width, height,
+    d_images (device pointer), matrices (projections x 12) and d_volume
+    (device pointer to N^3 floats)."""
+
+    def __init__(self, jobs: list[dict], cfg: LolaCudaConfig | None = None, **cfg_kw):
+        from ._native import LolaCudaJob
+        self.lib = load_lolacuda()
+        arr = (LolaCudaJob * len(jobs))()
+        self._mats = []
+        for i, j in enumerate(jobs):
+            m = np.ascontiguousarray(j["matrices"], np.float64).reshape(-1, 12)
+            self._mats.append(m)
+            arr[i].geometry = LolaCudaGeometry(j["n"], j["width"], j["height"], j["voxel_size"],
+                                               j["origin_index"], 0, 0)
+            arr[i].projections = m.shape[0]
+            arr[i].d_images = j["d_images"]
+            arr[i].h_matrices = m.ctypes.data
+            arr[i].d_volume = j["d_volume"]
+        self.cfg = cfg if cfg is not None else config(**cfg_kw)
+        h = C.c_void_p()
+        check(self.lib.lolaCudaBatchCreate(arr, len(jobs), C.byref(self.cfg), C.byref(h)),
+              "batch create")
+        self.handle = h
+
+    def run(self) -> None:
+        check(self.lib.lolaCudaBatchRun(self.handle), "batch run")
+
+    def synchronize(self) -> None:
+        check(self.lib.lolaCudaBatchSynchronize(self.handle), "batch synchronize")
+
+    def info(self):
+        from ._native import LolaCudaBatchInfo
+        i = LolaCudaBatchInfo()
+        check(self.lib.lolaCudaBatchGetInfo(self.handle, C.byref(i)), "batch info")
+        return i
+
+    def close(self) -> None:
+        if getattr(self, "handle", None):
+            self.lib.lolaCudaBatchDestroy(self.handle)
             self.handle = None
 
     def __enter__(self):
