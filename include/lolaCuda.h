@@ -116,8 +116,15 @@ typedef struct {
                             memory with tensor copies where it fits; 0: gather
                             through the load / texture path (default: measured
                             faster on GB300 at N=1024) */
-  int32_t reserved[6];
+  int32_t batchMode;     /* batched reconstructions: LOLA_BATCH_* */
+  int32_t batchBranches; /* LOLA_BATCH_BRANCHES: concurrent graph branches (0 = 16) */
+  int32_t reserved[4];
 } LolaCudaConfig;
+
+enum {
+  LOLA_BATCH_BRANCHES = 0,  /* per-job pass launches in parallel graph branches */
+  LOLA_BATCH_PERSISTENT = 1 /* one persistent pass launch per wave over all jobs */
+};
 
 /* Defaults: FP32 storage, plain accumulation, batch 16, 8 voxels per thread,
  * 8 rows per block, syncEachCall 1, exitOnError 1, no stats, device 0,

@@ -49,7 +49,9 @@ class LolaCudaConfig(C.Structure):
                 ("collectStats", C.c_int32),
                 ("device", C.c_int32),
                 ("staging", C.c_int32),
-                ("reserved", C.c_int32 * 6)]
+                ("batchMode", C.c_int32),
+                ("batchBranches", C.c_int32),
+                ("reserved", C.c_int32 * 4)]
 
 
 class LolaCudaGeometry(C.Structure):
@@ -212,7 +214,8 @@ def config(storage: str | None = None, accumulation: str | None = None,
            batch: int | None = None, voxels_per_thread: int | None = None,
            rows_per_block: int | None = None, sync_each_call: int | None = None,
            exit_on_error: int = 0, collect_stats: int | None = None, device: int | None = None,
-           staging: int | None = None) -> LolaCudaConfig:
+           staging: int | None = None, batch_mode: int | None = None,
+           batch_branches: int | None = None) -> LolaCudaConfig:
     """A LolaCudaConfig from the library's defaults (which honour the
     LOLACUDA_* environment overrides) with the given fields replaced.
     exit_on_error defaults to 0 here: Python callers want exceptions."""
@@ -225,7 +228,8 @@ def config(storage: str | None = None, accumulation: str | None = None,
     for name, value in (("batch", batch), ("voxelsPerThread", voxels_per_thread),
                         ("rowsPerBlock", rows_per_block), ("syncEachCall", sync_each_call),
                         ("exitOnError", exit_on_error), ("collectStats", collect_stats),
-                        ("device", device), ("staging", staging)):
+                        ("device", device), ("staging", staging), ("batchMode", batch_mode),
+                        ("batchBranches", batch_branches)):
         if value is not None:
             setattr(c, name, value)
     return c

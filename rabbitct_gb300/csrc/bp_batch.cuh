@@ -43,93 +43,108 @@ __global__ void __launch_bounds__(256) batchPackKernel(const LolaBatchWave w)
     Layout<S>::store(J.ring, o, px(u, v), 0.f, 0.f, 0.f);
 }
 
+/* Resident blocks per SM for the batched pass; its per-job geometry lives in
+ * registers rather than the constant bank, so it needs more of them than
+ * passKernel (a build-time tuning knob). */
+#ifndef LOLA_BATCH_MIN_BLOCKS
+#define LOLA_BATCH_MIN_BLOCKS 4
+#endif
+
 template <int S, bool KAHAN>
-__global__ void __launch_bounds__(256, 6) batchPassKernel(const LolaBatchWave w)
+__global__ void __launch_bounds__(256, LOLA_BATCH_MIN_BLOCKS) batchPassKernel(const LolaBatchWave w)
 {
   constexpr int VPT = 8, ROWS = 8;
   __shared__ TileProj sp[LOLA_MAX_BATCH];
-  __shared__ long long itemS;
+  /* the current work item: its job's descriptor and tile, shared by the
+     block so the per-voxel loop keeps only what passKernel keeps */
+  __shared__ LolaBatchJob J;
+  __shared__ int itemJob, itemCount, itemX0, itemY0, itemZ0, itemDone;
   const int tid = threadIdx.y * 32 + threadIdx.x;
   const float fi = (float)threadIdx.x, fj = (float)threadIdx.y;
   for (;;) {
-    if (tid == 0)
-      itemS = atomicAdd(w.counter, 1);
+    if (tid == 0) {
+      const long long item = atomicAdd(w.counter, 1);
+      itemDone = item >= w.totalItems;
+      if (!itemDone) {
+        /* job of the item: last j with tilePrefix[j] <= item */
+        int lo = 0, hi = w.njobs - 1;
+        while (lo < hi) {
+          const int mid = (lo + hi + 1) >> 1;
+          if (w.tilePrefix[mid] <= item)
+            lo = mid;
+          else
+            hi = mid - 1;
+        }
+        J = w.jobs[lo];
+        long long t = item - w.tilePrefix[lo];
+        itemJob = lo;
+        itemCount = min(w.b, J.nproj - w.wave * w.b);
+        itemX0 = (int)(t % J.tilesX) * 32;
+        t /= J.tilesX;
+        itemY0 = (int)(t % J.tilesY) * ROWS;
+        itemZ0 = (int)(t / J.tilesY) * VPT;
+      }
+    }
     __syncthreads();
-    const long long item = itemS;
-    __syncthreads(); /* every thread holds the item before tid 0 takes the next */
-    if (item >= w.totalItems)
+    if (itemDone)
       break;
-    /* job of the item: last j with tilePrefix[j] <= item */
-    int lo = 0, hi = w.njobs - 1;
-    while (lo < hi) {
-      const int mid = (lo + hi + 1) >> 1;
-      if (w.tilePrefix[mid] <= item)
-        lo = mid;
-      else
-        hi = mid - 1;
-    }
-    const LolaBatchJob &J = w.jobs[lo];
-    const int count = min(w.b, J.nproj - w.wave * w.b);
-    if (count <= 0)
-      continue;
-    long long t = item - w.tilePrefix[lo];
-    const int tx = (int)(t % J.tilesX);
-    t /= J.tilesX;
-    const int ty = (int)(t % J.tilesY);
-    const int tz = (int)(t / J.tilesY);
-    const int N = J.N;
-    const int x0 = tx * 32, y0 = ty * ROWS, z0 = tz * VPT;
-
-    TileGeom g;
-    g.N = N;
-    g.zEnd = N;
-    g.voxelSize = J.voxelSize;
-    g.originIndex = J.originIndex;
-    g.width = J.width;
-    g.height = J.height;
-    g.margin = J.margin;
-    setupTileGeom<ROWS, VPT>(w.proj + (size_t)lo * w.b, count, g, sp, tid, 32 * ROWS, x0, y0, z0);
-
-    PassArgs a;
-    a.ring = J.ring;
-    a.slotBytes = J.slotBytes;
-    a.volume = J.volume;
-    a.tileCounters = nullptr;
-    a.width = J.width;
-    a.height = J.height;
-    a.margin = J.margin;
-    a.pitch = J.pitch;
-    a.rows = J.rows;
-
-    const int x = x0 + threadIdx.x, y = y0 + threadIdx.y;
-    const bool inXY = (x < N) && (y < N);
-    const size_t slice = (size_t)N * (size_t)N;
-    float *vcol = J.volume + ((size_t)z0 * N + (size_t)(inXY ? y : 0)) * (size_t)N +
-                  (inXY ? x : 0);
-    float acc[VPT], comp[VPT];
+    const int count = itemCount;
+    if (count > 0) {
+      const int x0 = itemX0, y0 = itemY0, z0 = itemZ0;
+      TileGeom g;
+      g.N = J.N;
+      g.zEnd = J.N;
+      g.voxelSize = J.voxelSize;
+      g.originIndex = J.originIndex;
+      g.width = J.width;
+      g.height = J.height;
+      g.margin = J.margin;
+      setupTileGeom<ROWS, VPT>(w.proj + (size_t)itemJob * w.b, count, g, sp, tid, 32 * ROWS,
+          x0, y0, z0);
+      const int N = J.N;
+      const int x = x0 + threadIdx.x, y = y0 + threadIdx.y;
+      const bool inXY = (x < N) && (y < N);
+      const size_t slice = (size_t)N * (size_t)N;
+      float acc[VPT], comp[VPT];
+      {
+        const float *vcol = J.volume + ((size_t)z0 * N + (size_t)(inXY ? y : 0)) * (size_t)N +
+                            (inXY ? x : 0);
 #pragma unroll
-    for (int k = 0; k < VPT; ++k) {
-      acc[k] = (inXY && z0 + k < N) ? vcol[k * slice] : 0.0f;
-      comp[k] = 0.0f;
-    }
-    for (int p = 0; p < count; ++p) {
-      const int mode = sp[p].mode;
-      if (mode == MODE_SKIP)
-        continue;
-      const TileProj tp = sp[p];
-      const void *img = J.ring + (size_t)tp.slot * J.slotBytes;
-      const unsigned long long tex =
-          (Layout<S>::kTex || Layout<S>::kMixed) ? J.tex[tp.slot] : 0ull;
-      if (mode == MODE_FAST)
-        applyProjection<S, VPT, KAHAN, false>(tp, img, tex, a, fi, fj, acc, comp);
-      else
-        applyProjection<S, VPT, KAHAN, true>(tp, img, tex, a, fi, fj, acc, comp);
-    }
+        for (int k = 0; k < VPT; ++k) {
+          acc[k] = (inXY && z0 + k < N) ? vcol[k * slice] : 0.0f;
+          comp[k] = 0.0f;
+        }
+      }
+      /* read through a volatile view: re-read per projection from shared
+         memory instead of pinned in registers across the loop */
+      const volatile LolaBatchJob *Jv = &J;
+      for (int p = 0; p < count; ++p) {
+        const int mode = sp[p].mode;
+        if (mode == MODE_SKIP)
+          continue;
+        const TileProj tp = sp[p];
+        PassArgs a;
+        a.width = Jv->width;
+        a.height = Jv->height;
+        a.margin = Jv->margin;
+        a.pitch = Jv->pitch;
+        a.rows = Jv->rows;
+        const void *img = Jv->ring + (size_t)tp.slot * Jv->slotBytes;
+        const unsigned long long tex =
+            (Layout<S>::kTex || Layout<S>::kMixed) ? Jv->tex[tp.slot] : 0ull;
+        if (mode == MODE_FAST)
+          applyProjection<S, VPT, KAHAN, false>(tp, img, tex, a, fi, fj, acc, comp);
+        else
+          applyProjection<S, VPT, KAHAN, true>(tp, img, tex, a, fi, fj, acc, comp);
+      }
+      float *vcol = J.volume + ((size_t)z0 * N + (size_t)(inXY ? y : 0)) * (size_t)N +
+                    (inXY ? x : 0);
 #pragma unroll
-    for (int k = 0; k < VPT; ++k)
-      if (inXY && z0 + k < N)
-        vcol[k * slice] = KAHAN ? (acc[k] - comp[k]) : acc[k];
-    __syncthreads(); /* sp[] is rewritten by the next item's setup */
+      for (int k = 0; k < VPT; ++k)
+        if (inXY && z0 + k < N)
+          vcol[k * slice] = KAHAN ? (acc[k] - comp[k]) : acc[k];
+    }
+    __syncthreads(); /* J, sp[] and the item fields are rewritten next */
   }
 }
 

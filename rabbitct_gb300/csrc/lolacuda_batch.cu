@@ -12,6 +12,7 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <algorithm>
 #include <vector>
 
 #include <cuda_runtime.h>
@@ -22,6 +23,8 @@
 struct LolaCudaBatch {
   int device = 0;
   cudaStream_t stream = nullptr;
+  std::vector<cudaStream_t> branches;
+  std::vector<cudaEvent_t> events;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   LolaCudaConfig cfg;
@@ -78,6 +81,10 @@ void release(LolaCudaBatch *bt)
   cudaFree(bt->d_proj);
   cudaFree(bt->d_counters);
   cudaFree(bt->d_tex);
+  for (cudaStream_t b : bt->branches)
+    cudaStreamDestroy(b);
+  for (cudaEvent_t e : bt->events)
+    cudaEventDestroy(e);
   if (bt->stream)
     cudaStreamDestroy(bt->stream);
   delete bt;
@@ -91,6 +98,98 @@ void release(LolaCudaBatch *bt)
       return 0;                                                                           \
     }                                                                                     \
   } while (0)
+
+
+/* LOLA_BATCH_BRANCHES: each job's waves (pack, pass) chained in one of K
+ * parallel branches of the captured graph; jobs assigned largest first to the
+ * least loaded branch. */
+int captureBranches(LolaCudaBatch *bt, const LolaCudaJob *jobs,
+    const std::vector<LolaBatchJob> &hj, const std::vector<unsigned long long> &tex)
+{
+  const int nj = bt->njobs, b = bt->b;
+  int K = bt->cfg.batchBranches > 0 ? bt->cfg.batchBranches : 16;
+  K = K > nj ? nj : K;
+  std::vector<int> order(nj);
+  for (int j = 0; j < nj; ++j)
+    order[j] = j;
+  auto work = [&](int j) { return (double)hj[j].N * hj[j].N * hj[j].N * hj[j].nproj; };
+  std::sort(order.begin(), order.end(), [&](int a, int c) { return work(a) > work(c); });
+  std::vector<std::vector<int>> lanes(K);
+  std::vector<double> load(K, 0.0);
+  for (int j : order) {
+    int k = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+    lanes[k].push_back(j);
+    load[k] += work(j);
+  }
+  bt->branches.resize(K);
+  bt->events.resize(K + 1);
+  for (int k = 0; k < K; ++k)
+    BT_TRY(cudaStreamCreateWithFlags(&bt->branches[k], cudaStreamNonBlocking));
+  for (int k = 0; k <= K; ++k)
+    BT_TRY(cudaEventCreateWithFlags(&bt->events[k], cudaEventDisableTiming));
+
+  BT_TRY(cudaStreamBeginCapture(bt->stream, cudaStreamCaptureModeThreadLocal));
+  cudaError_t e = cudaEventRecord(bt->events[K], bt->stream);
+  int rc = 0;
+  for (int k = 0; k < K && e == cudaSuccess && rc == 0; ++k) {
+    cudaStream_t st = bt->branches[k];
+    e = cudaStreamWaitEvent(st, bt->events[K], 0);
+    for (int j : lanes[k]) {
+      const LolaBatchJob &J = hj[j];
+      LolaStoreDesc sd;
+      memset(&sd, 0, sizeof(sd));
+      sd.storage = bt->cfg.storage;
+      sd.elemBytes = (int32_t)(J.slotBytes / J.slotElems);
+      sd.margin = J.margin;
+      sd.pitch = J.pitch;
+      sd.rows = J.rows;
+      sd.width = J.width;
+      sd.height = J.height;
+      sd.slotElems = J.slotElems;
+      for (int s = 0; s < b && !tex.empty(); ++s)
+        sd.texObjects[s] = tex[(size_t)j * b + s];
+      const size_t img = (size_t)J.width * J.height;
+      for (int w0 = 0; w0 < J.nproj && e == cudaSuccess && rc == 0; w0 += b) {
+        const int n = J.nproj - w0 < b ? J.nproj - w0 : b;
+        rc = lolaLaunchPack(&sd, J.images + (size_t)w0 * img, img, J.ring, 0, n, st);
+        if (rc != 0)
+          break;
+        LolaPassParams P;
+        memset(&P, 0, sizeof(P));
+        P.N = J.N;
+        P.count = n;
+        P.zBegin = 0;
+        P.zEnd = J.N;
+        P.voxelSize = J.voxelSize;
+        P.originIndex = J.originIndex;
+        P.accumulation = bt->cfg.accumulation;
+        P.voxelsPerThread = 8;
+        P.rowsPerBlock = 8;
+        for (int i = 0; i < n; ++i) {
+          const double *m = jobs[j].h_matrices + 12 * (size_t)(w0 + i);
+          memcpy(P.proj[i].a, m, 12 * sizeof(double));
+          for (int ax = 0; ax < 3; ++ax)
+            for (int c = 0; c < 3; ++c)
+              P.proj[i].step[ax][c] = (float)(m[ax * 3 + c] * (double)J.voxelSize);
+          P.proj[i].slot = i;
+        }
+        rc = lolaLaunchBackproject(&sd, &P, nullptr, J.ring, J.volume, nullptr, st);
+        bt->launches += 2;
+      }
+    }
+    if (e == cudaSuccess)
+      e = cudaEventRecord(bt->events[k], st);
+    if (e == cudaSuccess)
+      e = cudaStreamWaitEvent(bt->stream, bt->events[k], 0);
+  }
+  cudaError_t ce = cudaStreamEndCapture(bt->stream, &bt->graph);
+  if (e != cudaSuccess || rc != 0 || ce != cudaSuccess)
+    return lolaSetError("batch: capture failed: %s / %s / %s", cudaGetErrorString(e),
+        cudaGetErrorString((cudaError_t)rc), cudaGetErrorString(ce));
+  BT_TRY(cudaGraphInstantiate(&bt->exec, bt->graph, 0));
+  bt->blocks = 0;
+  return 1;
+}
 
 int build(LolaCudaBatch *bt, const LolaCudaJob *jobs)
 {
@@ -177,6 +276,9 @@ int build(LolaCudaBatch *bt, const LolaCudaJob *jobs)
   BT_TRY(cudaMalloc(&bt->d_jobs, (size_t)nj * sizeof(LolaBatchJob)));
   BT_TRY(cudaMemcpy(bt->d_jobs, hj.data(), (size_t)nj * sizeof(LolaBatchJob),
       cudaMemcpyHostToDevice));
+
+  if (bt->cfg.batchMode == LOLA_BATCH_BRANCHES)
+    return captureBranches(bt, jobs, hj, texHandles);
 
   /* per wave: work lists over the jobs still active and their projections */
   const int W = bt->waves;

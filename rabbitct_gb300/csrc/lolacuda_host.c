@@ -120,6 +120,8 @@ void lolaCudaDefaultConfig(LolaCudaConfig *c)
   c->syncEachCall = envInt("LOLACUDA_SYNC", c->syncEachCall);
   c->exitOnError = envInt("LOLACUDA_EXIT", c->exitOnError);
   c->staging = envInt("LOLACUDA_STAGING", 0);
+  c->batchMode = envInt("LOLACUDA_BATCH_MODE", LOLA_BATCH_BRANCHES);
+  c->batchBranches = envInt("LOLACUDA_BATCH_BRANCHES", 16);
 }
 
 static int validateConfig(const LolaCudaConfig *c)

@@ -32,8 +32,9 @@ def scans():
     return out
 
 
+@pytest.mark.parametrize("mode", [0, 1])  # LOLA_BATCH_BRANCHES, LOLA_BATCH_PERSISTENT
 @pytest.mark.parametrize("storage", ["f32", "f16qx", "tex16", "f16"])
-def test_batch_matches_plans_and_oracle(scans, storage):
+def test_batch_matches_plans_and_oracle(scans, storage, mode):
     from rabbitct_gb300.lolacuda import Batch, DeviceBuffer, Plan
     bufs, jobs = [], []
     for n, vs, o, scan in scans:
@@ -43,9 +44,11 @@ def test_batch_matches_plans_and_oracle(scans, storage):
         jobs.append(dict(n=n, voxel_size=vs, origin_index=o, width=scan.width,
                          height=scan.height, d_images=d_img.ptr, matrices=scan.matrices,
                          d_volume=d_vol.ptr))
-    with Batch(jobs, storage=storage, batch=4) as bt:
+    with Batch(jobs, storage=storage, batch=4, batch_mode=mode, batch_branches=3) as bt:
         info = bt.info()
-        assert info.jobs == len(JOBS) and info.waves == 3 and info.launchesPerRun == 6
+        waves = [-(-p // 4) for _, _, _, p, _ in JOBS]
+        assert info.jobs == len(JOBS) and info.waves == max(waves)
+        assert info.launchesPerRun == (2 * max(waves) if mode == 1 else 2 * sum(waves))
         bt.run()
         bt.synchronize()
         first = [v.to_array((n, n, n), np.float32) for (_, v), (n, *_rest) in zip(bufs, scans)]
