@@ -75,6 +75,9 @@ def parse_args():
     ap.add_argument("--batch", type=int, default=16)
     ap.add_argument("--vpt", type=int, default=8)
     ap.add_argument("--rows", type=int, default=8)
+    ap.add_argument("--autotune", type=int, default=1,
+                    help="1: pick tile shape / batch / staging with lolaCudaAutotune on the "
+                         "first 32 projections before timing (untimed)")
     ap.add_argument("--staging", type=int, default=None,
                     help="1/0: force shared-memory staging on/off (default: library default)")
     ap.add_argument("--e2e-steps", type=int, default=2)
@@ -282,12 +285,25 @@ def total_updates(args, scan, dist) -> float:
     return per if args.shard == "slabs" else per * dist.world
 
 
+def tuned_config(args, dist, scan, vs, o, d_images, storage):
+    """The configuration a run uses: autotuned on the first 32 projections
+    (untimed) or taken from the command line."""
+    from rabbitct_gb300.lolacuda import autotune, config
+    base = config(storage=storage, batch=args.batch, voxels_per_thread=args.vpt,
+                  rows_per_block=args.rows, staging=args.staging)
+    if not args.autotune:
+        return base, None
+    cfg, tried = autotune(args.n, vs, o, scan.width, scan.height, d_images.ptr,
+                          scan.matrices[:32], cfg=base, slab=my_slab(args, dist))
+    return cfg, tried
+
+
 def time_device(args, dist, lib_mod, scan, vs, o, d_images, storage, clocks=None):
     from rabbitct_gb300.lolacuda import Plan
     W, H = scan.width, scan.height
-    with Plan(args.n, vs, o, W, H, storage=storage, batch=args.batch,
-              voxels_per_thread=args.vpt, rows_per_block=args.rows, collect_stats=1,
-              staging=args.staging, slab=my_slab(args, dist)) as p:
+    cfg, tried = tuned_config(args, dist, scan, vs, o, d_images, storage)
+    cfg.collectStats = 1
+    with Plan(args.n, vs, o, W, H, cfg=cfg, slab=my_slab(args, dist)) as p:
         for _ in range(args.warmup):
             p.zero()
             p.backproject_device(d_images.ptr, W * H, scan.matrices)
@@ -308,11 +324,19 @@ def time_device(args, dist, lib_mod, scan, vs, o, d_images, storage, clocks=None
         st = p.stats()
     ms_max = dist.max(ms)
     updates = total_updates(args, scan, dist) * args.steps
-    return {"ms": ms_max, "gups": updates / (ms_max * 1e-3) / 1e9, "stats": st, "clocks": clk}
+    chosen = {"storage": storage, "voxels_per_thread": cfg.voxelsPerThread,
+              "rows_per_block": cfg.rowsPerBlock, "batch": cfg.batch, "staging": cfg.staging,
+              "autotuned": bool(args.autotune),
+              "candidates_timed": 0 if tried is None else sum(1 for t in tried if t[3] > 0)}
+    return {"ms": ms_max, "gups": updates / (ms_max * 1e-3) / 1e9, "stats": st, "clocks": clk,
+            "cfg": cfg, "chosen": chosen}
 
 
-def roofline(args, lib, storage, st, probes) -> dict:
-    tile = 32 * args.rows * args.vpt
+def roofline(args, lib, storage, st, probes, cfg=None) -> dict:
+    rows = cfg.rowsPerBlock if cfg is not None else args.rows
+    vpt = cfg.voxelsPerThread if cfg is not None else args.vpt
+    batch = cfg.batch if cfg is not None else args.batch
+    tile = 32 * rows * vpt
     computed = (st.tilePassesFast + st.tilePassesSlow) * tile
     launches = max(1, st.passes)
     avg_ms = st.passMs / launches
@@ -337,7 +361,7 @@ def roofline(args, lib, storage, st, probes) -> dict:
     elem = {"f32": 4, "f16": 2, "bf16": 2, "f32q": 16, "f16q": 8, "bf16q": 8, "tex32": 4,
             "tex16": 2, "f16qx": 8, "f32qx": 16}[storage]
     vol_bytes = 8.0 * args.n ** 3
-    proj_bytes = args.batch * (args.width + 128) * (args.height + 128) * elem
+    proj_bytes = batch * (args.width + 128) * (args.height + 128) * elem
     hbm_gbs = (vol_bytes + proj_bytes) / (avg_ms * 1e-3) / 1e9
     peaks = {}
     mp = ROOT / "MEASURED_PEAKS.json"
@@ -471,6 +495,11 @@ def run_gpu(args, rank, world, local):
     if not args.no_fp32 and args.fp32_storage != args.storage:
         fp32 = time_device(args, dist, lib, scan, vs, o, d_images, args.fp32_storage)
     d_images.free()
+    if args.autotune:
+        args.vpt = head["cfg"].voxelsPerThread
+        args.rows = head["cfg"].rowsPerBlock
+        args.batch = head["cfg"].batch
+        args.staging = head["cfg"].staging
     e2e = None if args.no_e2e else time_e2e(args, dist, scan, vs, o, args.storage)
 
     if rank != 0:
@@ -487,14 +516,16 @@ def run_gpu(args, rank, world, local):
         "config": workload_config(args, args.storage),
         "gpu_launches": int(st.passes + st.packs),
         "clocks": head["clocks"],
-        "roofline": roofline(args, lib, args.storage, st, probes),
+        "roofline": roofline(args, lib, args.storage, st, probes, head["cfg"]),
+        "tuned": head["chosen"],
     }
     if fp32 is not None:
         line["fp32_path"] = {"value": fp32["gups"], "unit": "GUPS",
                              "storage": args.fp32_storage,
                              "ms_per_step": fp32["ms"] / args.steps,
                              "roofline": roofline(args, lib, args.fp32_storage, fp32["stats"],
-                                                  probes)}
+                                                  probes, fp32["cfg"]),
+                             "tuned": fp32["chosen"]}
         line["fp16_over_fp32"] = head["gups"] / fp32["gups"]
     if e2e is not None:
         line["e2e"] = e2e

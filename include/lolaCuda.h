@@ -118,7 +118,10 @@ typedef struct {
                             faster on GB300 at N=1024) */
   int32_t batchMode;     /* batched reconstructions: LOLA_BATCH_* */
   int32_t batchBranches; /* LOLA_BATCH_BRANCHES: concurrent graph branches (0 = 16) */
-  int32_t reserved[4];
+  int32_t batchTune;     /* LOLA_BATCH_BRANCHES: time the tile shapes once per distinct
+                            (N, detector) class at create and use the fastest for
+                            its jobs (1), or use voxelsPerThread x rowsPerBlock (0) */
+  int32_t reserved[3];
 } LolaCudaConfig;
 
 enum {
@@ -304,6 +307,30 @@ int lolaCudaSlab(int problemSize, int rank, int ranks, int align, int32_t *slice
 int lolaCudaBackprojectNoAlloc(const LolaCudaGeometry *geometry, const LolaCudaConfig *config,
     float *d_volume, const float *d_images, size_t imageStride, const double *h_matrices,
     int count, void *stream);
+
+/* ---- Autotuning --------------------------------------------------------------
+ * No counterpart in the reference (compile-time VECTORSIZE / BLOCKING_FACTOR).
+ * Times candidate execution parameters — tile shape (voxels per thread x rows
+ * per block), projections per pass and shared-memory staging — on the
+ * caller's own geometry and projections (count of them, device-resident,
+ * FP32) and writes the fastest into *config.  Storage and accumulation are
+ * taken from *config unchanged, so the result keeps its accuracy.  Each
+ * candidate is timed with CUDA events after a warm-up, on a scratch plan. */
+typedef struct {
+  int32_t voxelsPerThread, rowsPerBlock, batch, staging;
+  double ms;                 /* time for the count projections; < 0: not run */
+} LolaCudaTuneCandidate;
+
+#define LOLA_TUNE_MAX_CANDIDATES 64
+
+typedef struct {
+  int32_t candidates;
+  int32_t best;
+  LolaCudaTuneCandidate tried[LOLA_TUNE_MAX_CANDIDATES];
+} LolaCudaTuneReport;
+
+int lolaCudaAutotune(const LolaCudaGeometry *geometry, const float *d_images, size_t imageStride,
+    const double *h_matrices, int count, LolaCudaConfig *config, LolaCudaTuneReport *report);
 
 /* Small device-memory helpers so hosts without a CUDA binding (ctypes, cgo)
  * can stage device-resident inputs. */

@@ -51,7 +51,8 @@ class LolaCudaConfig(C.Structure):
                 ("staging", C.c_int32),
                 ("batchMode", C.c_int32),
                 ("batchBranches", C.c_int32),
-                ("reserved", C.c_int32 * 4)]
+                ("batchTune", C.c_int32),
+                ("reserved", C.c_int32 * 3)]
 
 
 class LolaCudaGeometry(C.Structure):
@@ -79,6 +80,16 @@ class LolaCudaBatchInfo(C.Structure):
     _fields_ = [("jobs", C.c_int32), ("waves", C.c_int32), ("blocks", C.c_int32),
                 ("launchesPerRun", C.c_int32), ("voxelUpdates", C.c_double),
                 ("ringBytes", C.c_size_t)]
+
+
+class LolaCudaTuneCandidate(C.Structure):
+    _fields_ = [("voxelsPerThread", C.c_int32), ("rowsPerBlock", C.c_int32),
+                ("batch", C.c_int32), ("staging", C.c_int32), ("ms", C.c_double)]
+
+
+class LolaCudaTuneReport(C.Structure):
+    _fields_ = [("candidates", C.c_int32), ("best", C.c_int32),
+                ("tried", LolaCudaTuneCandidate * 64)]
 
 
 class LolaCudaStats(C.Structure):
@@ -145,6 +156,8 @@ _SIGNATURES = [
     ("lolaCudaBatchStream", _P, [_P]),
     ("lolaCudaBatchGetInfo", C.c_int, [_P, C.POINTER(LolaCudaBatchInfo)]),
     ("lolaCudaBatchDestroy", C.c_int, [_P]),
+    ("lolaCudaAutotune", C.c_int, [C.POINTER(LolaCudaGeometry), _P, C.c_size_t, _P, C.c_int,
+                                   C.POINTER(LolaCudaConfig), C.POINTER(LolaCudaTuneReport)]),
     ("lolaCudaHostAlloc", _P, [C.c_size_t]),
     ("lolaCudaHostFree", C.c_int, [_P]),
     ("lolaCudaProbeIssueRate", C.c_double, []),
@@ -215,7 +228,7 @@ def config(storage: str | None = None, accumulation: str | None = None,
            rows_per_block: int | None = None, sync_each_call: int | None = None,
            exit_on_error: int = 0, collect_stats: int | None = None, device: int | None = None,
            staging: int | None = None, batch_mode: int | None = None,
-           batch_branches: int | None = None) -> LolaCudaConfig:
+           batch_branches: int | None = None, batch_tune: int | None = None) -> LolaCudaConfig:
     """A LolaCudaConfig from the library's defaults (which honour the
     LOLACUDA_* environment overrides) with the given fields replaced.
     exit_on_error defaults to 0 here: Python callers want exceptions."""
@@ -229,7 +242,7 @@ def config(storage: str | None = None, accumulation: str | None = None,
                         ("rowsPerBlock", rows_per_block), ("syncEachCall", sync_each_call),
                         ("exitOnError", exit_on_error), ("collectStats", collect_stats),
                         ("device", device), ("staging", staging), ("batchMode", batch_mode),
-                        ("batchBranches", batch_branches)):
+                        ("batchBranches", batch_branches), ("batchTune", batch_tune)):
         if value is not None:
             setattr(c, name, value)
     return c

@@ -103,10 +103,67 @@ void release(LolaCudaBatch *bt)
 /* LOLA_BATCH_BRANCHES: each job's waves (pack, pass) chained in one of K
  * parallel branches of the captured graph; jobs assigned largest first to the
  * least loaded branch. */
+/* Tile shape per job: the configured one, or with batchTune the fastest of
+ * the compiled shapes, timed once per distinct (N, detector) class on that
+ * class's first projections with a scratch plan. */
+int chooseShapes(LolaCudaBatch *bt, const LolaCudaJob *jobs, const std::vector<LolaBatchJob> &hj,
+    std::vector<int> &vpt, std::vector<int> &rows)
+{
+  const int nj = bt->njobs;
+  vpt.assign(nj, bt->cfg.voxelsPerThread);
+  rows.assign(nj, bt->cfg.rowsPerBlock);
+  if (!bt->cfg.batchTune)
+    return 1;
+  static const int shapes[][2] = { { 8, 8 }, { 8, 4 }, { 16, 4 }, { 16, 8 }, { 4, 8 } };
+  std::vector<int> done(nj, 0);
+  for (int j = 0; j < nj; ++j) {
+    if (done[j] || hj[j].nproj <= 0)
+      continue;
+    const int count = hj[j].nproj < 2 * bt->b ? hj[j].nproj : 2 * bt->b;
+    double bestMs = 1e300;
+    int bv = bt->cfg.voxelsPerThread, br = bt->cfg.rowsPerBlock;
+    for (const auto &sh : shapes) {
+      LolaCudaConfig c = bt->cfg;
+      c.voxelsPerThread = sh[0];
+      c.rowsPerBlock = sh[1];
+      c.staging = 0;
+      c.collectStats = 0;
+      LolaCudaGeometry g = jobs[j].geometry;
+      g.sliceBegin = g.sliceCount = 0;
+      LolaCudaPlan *p = nullptr;
+      if (!lolaCudaPlanCreate(&g, &c, &p))
+        continue;
+      double ms = -1.0;
+      const size_t img = (size_t)hj[j].width * hj[j].height;
+      if (lolaCudaPlanBackprojectDevice(p, hj[j].images, img, jobs[j].h_matrices, count) &&
+          lolaCudaPlanSynchronize(p) && lolaCudaPlanTimerStart(p) &&
+          lolaCudaPlanBackprojectDevice(p, hj[j].images, img, jobs[j].h_matrices, count))
+        lolaCudaPlanTimerStop(p, &ms);
+      lolaCudaPlanDestroy(p);
+      if (ms > 0.0 && ms < bestMs) {
+        bestMs = ms;
+        bv = sh[0];
+        br = sh[1];
+      }
+    }
+    for (int k = j; k < nj; ++k)
+      if (!done[k] && hj[k].N == hj[j].N && hj[k].width == hj[j].width &&
+          hj[k].height == hj[j].height) {
+        vpt[k] = bv;
+        rows[k] = br;
+        done[k] = 1;
+      }
+  }
+  return 1;
+}
+
 int captureBranches(LolaCudaBatch *bt, const LolaCudaJob *jobs,
     const std::vector<LolaBatchJob> &hj, const std::vector<unsigned long long> &tex)
 {
   const int nj = bt->njobs, b = bt->b;
+  std::vector<int> vpt, rows;
+  if (!chooseShapes(bt, jobs, hj, vpt, rows))
+    return 0;
   int K = bt->cfg.batchBranches > 0 ? bt->cfg.batchBranches : 16;
   K = K > nj ? nj : K;
   std::vector<int> order(nj);
@@ -163,8 +220,8 @@ int captureBranches(LolaCudaBatch *bt, const LolaCudaJob *jobs,
         P.voxelSize = J.voxelSize;
         P.originIndex = J.originIndex;
         P.accumulation = bt->cfg.accumulation;
-        P.voxelsPerThread = 8;
-        P.rowsPerBlock = 8;
+        P.voxelsPerThread = vpt[j];
+        P.rowsPerBlock = rows[j];
         for (int i = 0; i < n; ++i) {
           const double *m = jobs[j].h_matrices + 12 * (size_t)(w0 + i);
           memcpy(P.proj[i].a, m, 12 * sizeof(double));

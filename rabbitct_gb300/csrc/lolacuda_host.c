@@ -122,6 +122,7 @@ void lolaCudaDefaultConfig(LolaCudaConfig *c)
   c->staging = envInt("LOLACUDA_STAGING", 0);
   c->batchMode = envInt("LOLACUDA_BATCH_MODE", LOLA_BATCH_BRANCHES);
   c->batchBranches = envInt("LOLACUDA_BATCH_BRANCHES", 16);
+  c->batchTune = envInt("LOLACUDA_BATCH_TUNE", 1);
 }
 
 static int validateConfig(const LolaCudaConfig *c)
@@ -832,6 +833,65 @@ int lolaCudaPlanResetStats(LolaCudaPlan *p)
     return 0;
   memset(&p->stats, 0, sizeof(p->stats));
   CUDA_TRY(cudaMemset(p->d_counters, 0, 4 * sizeof(unsigned long long)));
+  return 1;
+}
+
+/* ---- autotuning ------------------------------------------------------------------ */
+
+int lolaCudaAutotune(const LolaCudaGeometry *g, const float *d_images, size_t imageStride,
+    const double *h_mats, int count, LolaCudaConfig *cfg, LolaCudaTuneReport *report)
+{
+  if (g == NULL || d_images == NULL || h_mats == NULL || cfg == NULL || count <= 0)
+    return setError("autotune: invalid arguments");
+  static const int shapes[][2] = { { 8, 8 }, { 8, 4 }, { 16, 4 }, { 16, 8 }, { 4, 8 } };
+  static const int batches[] = { 8, 16, 32 };
+  LolaCudaTuneReport local;
+  LolaCudaTuneReport *r = report ? report : &local;
+  memset(r, 0, sizeof(*r));
+  r->best = -1;
+  double bestMs = 1e300;
+  LolaCudaConfig best = *cfg;
+  for (int si = 0; si < 5; si++)
+    for (int bi = 0; bi < 3; bi++)
+      for (int staging = 0; staging <= 1; staging++) {
+        /* staging exists for 8 voxels per thread only */
+        if (staging && shapes[si][0] != 8)
+          continue;
+        if (r->candidates >= LOLA_TUNE_MAX_CANDIDATES)
+          break;
+        LolaCudaConfig c = *cfg;
+        c.voxelsPerThread = shapes[si][0];
+        c.rowsPerBlock = shapes[si][1];
+        c.batch = batches[bi] < count ? batches[bi] : count;
+        c.staging = staging;
+        c.collectStats = 0;
+        LolaCudaTuneCandidate *t = &r->tried[r->candidates++];
+        t->voxelsPerThread = c.voxelsPerThread;
+        t->rowsPerBlock = c.rowsPerBlock;
+        t->batch = c.batch;
+        t->staging = staging;
+        t->ms = -1.0;
+        LolaCudaPlan *p = NULL;
+        if (!lolaCudaPlanCreate(g, &c, &p))
+          continue;
+        double ms = -1.0;
+        /* one warm-up, then the timed run */
+        if (lolaCudaPlanBackprojectDevice(p, d_images, imageStride, h_mats, count) &&
+            lolaCudaPlanSynchronize(p) && lolaCudaPlanTimerStart(p) &&
+            lolaCudaPlanBackprojectDevice(p, d_images, imageStride, h_mats, count))
+          lolaCudaPlanTimerStop(p, &ms);
+        planRelease(p);
+        t->ms = ms;
+        if (ms > 0.0 && ms < bestMs) {
+          bestMs = ms;
+          best = c;
+          r->best = r->candidates - 1;
+        }
+      }
+  if (r->best < 0)
+    return setError("autotune: no candidate ran");
+  best.collectStats = cfg->collectStats;
+  *cfg = best;
   return 1;
 }
 

@@ -13,7 +13,8 @@ from . import _native
 from ._native import (LolaCudaConfig, LolaCudaGeometry, LolaCudaStats, Projection,
                       RabbitCtGlobalData, check, config, load_lolacuda)
 
-__all__ = ["Plan", "Batch", "DeviceBuffer", "GlobalData", "module_functions", "config", "slab"]
+__all__ = ["Plan", "Batch", "DeviceBuffer", "GlobalData", "module_functions", "config", "slab",
+           "autotune"]
 
 
 def slab(n: int, rank: int, ranks: int, align: int = 8) -> tuple[int, int]:
@@ -161,6 +162,24 @@ class Plan:
             self.close()
         except Exception:
             pass
+
+
+def autotune(n: int, voxel_size: float, origin_index: float, width: int, height: int,
+             d_images: int, matrices: np.ndarray, cfg: LolaCudaConfig | None = None,
+             slab: tuple[int, int] | None = None, **cfg_kw):
+    """lolaCudaAutotune: returns (tuned config, list of (shape, batch, staging, ms))."""
+    from ._native import LolaCudaTuneReport
+    lib = load_lolacuda()
+    c = cfg if cfg is not None else config(**cfg_kw)
+    b, k = (0, 0) if slab is None else slab
+    g = LolaCudaGeometry(n, width, height, voxel_size, origin_index, b, k)
+    m = np.ascontiguousarray(matrices, np.float64).reshape(-1, 12)
+    rep = LolaCudaTuneReport()
+    check(lib.lolaCudaAutotune(C.byref(g), d_images, width * height, m.ctypes.data, m.shape[0],
+                               C.byref(c), C.byref(rep)), "autotune")
+    tried = [((t.voxelsPerThread, t.rowsPerBlock), t.batch, t.staging, t.ms)
+             for t in rep.tried[:rep.candidates]]
+    return c, tried
 
 
 class Batch:

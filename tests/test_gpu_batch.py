@@ -44,7 +44,8 @@ def test_batch_matches_plans_and_oracle(scans, storage, mode):
         jobs.append(dict(n=n, voxel_size=vs, origin_index=o, width=scan.width,
                          height=scan.height, d_images=d_img.ptr, matrices=scan.matrices,
                          d_volume=d_vol.ptr))
-    with Batch(jobs, storage=storage, batch=4, batch_mode=mode, batch_branches=3) as bt:
+    with Batch(jobs, storage=storage, batch=4, batch_mode=mode, batch_branches=3,
+               batch_tune=0) as bt:
         info = bt.info()
         waves = [-(-p // 4) for _, _, _, p, _ in JOBS]
         assert info.jobs == len(JOBS) and info.waves == max(waves)
@@ -66,3 +67,46 @@ def test_batch_matches_plans_and_oracle(scans, storage, mode):
     for d_img, d_vol in bufs:
         d_img.free()
         d_vol.free()
+
+
+def test_tuned_batch_matches_oracle(scans):
+    """With per-class tile-shape tuning the shapes may differ from a plan's, so
+    the check is against the FP64 oracle."""
+    from rabbitct_gb300.lolacuda import Batch, DeviceBuffer
+    bufs, jobs = [], []
+    for n, vs, o, scan in scans:
+        d_img = DeviceBuffer.from_array(scan.images)
+        d_vol = DeviceBuffer.from_array(np.zeros((n, n, n), np.float32))
+        bufs.append((d_img, d_vol))
+        jobs.append(dict(n=n, voxel_size=vs, origin_index=o, width=scan.width,
+                         height=scan.height, d_images=d_img.ptr, matrices=scan.matrices,
+                         d_volume=d_vol.ptr))
+    with Batch(jobs, storage="f32", batch=4, batch_tune=1) as bt:
+        bt.run()
+        bt.synchronize()
+    for (n, vs, o, scan), (d_img, d_vol) in zip(scans, bufs):
+        got = d_vol.to_array((n, n, n), np.float32)
+        ref = oracle.bunny_f64(n, vs, o, scan.matrices, scan.images)
+        assert metrics.errors(got, ref)["rel_rmse"] <= 1e-5
+        d_img.free()
+        d_vol.free()
+
+
+def test_autotune_picks_a_measured_candidate(scans):
+    from rabbitct_gb300.lolacuda import DeviceBuffer, Plan, autotune
+    n, vs, o, scan = scans[3]
+    d_img = DeviceBuffer.from_array(scan.images)
+    cfg, tried = autotune(n, vs, o, scan.width, scan.height, d_img.ptr, scan.matrices,
+                          storage="f16qx")
+    ran = [t for t in tried if t[3] > 0]
+    assert len(ran) >= 10
+    best = min(ran, key=lambda t: t[3])
+    assert (cfg.voxelsPerThread, cfg.rowsPerBlock) == best[0]
+    assert cfg.batch == best[1] and cfg.staging == best[2] and cfg.storage == 8
+    with Plan(n, vs, o, scan.width, scan.height, cfg=cfg) as plan:
+        plan.backproject_device(d_img.ptr, scan.width * scan.height, scan.matrices)
+        plan.synchronize()
+        vol = plan.download()
+    d_img.free()
+    ref = oracle.bunny_f64(n, vs, o, scan.matrices, scan.images)
+    assert metrics.errors(vol, ref)["rel_rmse"] <= 1e-3
