@@ -308,6 +308,26 @@ int lolaCudaBackprojectNoAlloc(const LolaCudaGeometry *geometry, const LolaCudaC
     float *d_volume, const float *d_images, size_t imageStride, const double *h_matrices,
     int count, void *stream);
 
+/* ---- Reconstruction from a .rct file ---------------------------------------
+ * The input path of the reference runner (src/ctFileReader.c:47-61,
+ * src/rabbitRunner.c:267-287) without the runner: the projection records of
+ * a .rct file are read in chunks of `batch` into two page-locked buffers in
+ * turn, so disk reads overlap uploads and passes.  h_volume (N^3, host) is
+ * the starting volume and receives the result. */
+typedef struct {
+  double seconds;       /* wall time of the whole call */
+  double readSeconds;   /* time spent reading the file */
+  int64_t projections;
+  double gups;          /* N^3 x projections / seconds */
+  float hus[2];         /* the file's HU scaling factors */
+} LolaCudaFileReport;
+
+int lolaCudaReadRctHeader(const char *path, uint32_t *width, uint32_t *height, uint32_t *count,
+    float *hus);
+int lolaCudaReconstructFile(const char *path, int problemSize, float voxelSize,
+    float originIndex, const LolaCudaConfig *config, float *h_volume,
+    LolaCudaFileReport *report);
+
 /* ---- Autotuning --------------------------------------------------------------
  * No counterpart in the reference (compile-time VECTORSIZE / BLOCKING_FACTOR).
  * Times candidate execution parameters — tile shape (voxels per thread x rows

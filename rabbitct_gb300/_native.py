@@ -92,6 +92,11 @@ class LolaCudaTuneReport(C.Structure):
                 ("tried", LolaCudaTuneCandidate * 64)]
 
 
+class LolaCudaFileReport(C.Structure):
+    _fields_ = [("seconds", C.c_double), ("readSeconds", C.c_double),
+                ("projections", C.c_int64), ("gups", C.c_double), ("hus", C.c_float * 2)]
+
+
 class LolaCudaStats(C.Structure):
     _fields_ = [("passes", C.c_int64),
                 ("packs", C.c_int64),
@@ -158,6 +163,10 @@ _SIGNATURES = [
     ("lolaCudaBatchDestroy", C.c_int, [_P]),
     ("lolaCudaAutotune", C.c_int, [C.POINTER(LolaCudaGeometry), _P, C.c_size_t, _P, C.c_int,
                                    C.POINTER(LolaCudaConfig), C.POINTER(LolaCudaTuneReport)]),
+    ("lolaCudaReadRctHeader", C.c_int, [C.c_char_p, _P, _P, _P, _P]),
+    ("lolaCudaReconstructFile", C.c_int, [C.c_char_p, C.c_int, C.c_float, C.c_float,
+                                          C.POINTER(LolaCudaConfig), _P,
+                                          C.POINTER(LolaCudaFileReport)]),
     ("lolaCudaHostAlloc", _P, [C.c_size_t]),
     ("lolaCudaHostFree", C.c_int, [_P]),
     ("lolaCudaProbeIssueRate", C.c_double, []),

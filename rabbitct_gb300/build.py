@@ -29,7 +29,7 @@ CU_SOURCES = [
     "lolacuda_dispatch.cu", "lolacuda_probe.cu", "lolacuda_noalloc.cu",
     "lolacuda_geometry.cu", "lolacuda_verify.cu", "lolacuda_batch.cu",
 ]
-C_SOURCES = ["lolacuda_host.c"]
+C_SOURCES = ["lolacuda_host.c", "lolacuda_file.c"]
 
 
 def _cuda_home() -> Path:

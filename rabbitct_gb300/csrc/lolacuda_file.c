@@ -1,0 +1,162 @@
+/* Reconstruction straight from a RabbitCT .rct file (C99).
+ *
+ * File format (reference src/ctFileReader_types.h:11-15, src/ctFileReader.c:
+ * 47-61): a 20-byte header {u32 width, u32 height, u32 count, f32 hus[2]},
+ * then per projection 12 FP64 matrix values followed by width*height FP32
+ * pixels.  The reference runner reads one record at a time between timed
+ * module calls (src/rabbitRunner.c:275-279).  Here chunks of `batch` records
+ * are read into two page-locked buffers in turn: while the GPU uploads and
+ * backprojects chunk k (asynchronously, lolaCudaPlanBackprojectHost returns
+ * once the upload is done), the host reads chunk k+1 from disk.
+ */
+#define _POSIX_C_SOURCE 200809L
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <time.h>
+
+#include <cuda_runtime_api.h>
+
+#include "lolaCuda.h"
+#include "lolacuda_internal.h"
+
+static double nowSeconds(void)
+{
+  struct timespec ts;
+  clock_gettime(CLOCK_MONOTONIC, &ts);
+  return (double)ts.tv_sec + 1e-9 * (double)ts.tv_nsec;
+}
+
+typedef struct {
+  uint32_t width, height, count;
+  float hus[2];
+} RctHeader;
+
+int lolaCudaReadRctHeader(const char *path, uint32_t *width, uint32_t *height, uint32_t *count,
+    float *hus)
+{
+  FILE *f = fopen(path, "rb");
+  if (f == NULL)
+    return lolaSetError("cannot open %s", path);
+  unsigned char raw[20];
+  const size_t got = fread(raw, 1, sizeof(raw), f);
+  fclose(f);
+  if (got != sizeof(raw))
+    return lolaSetError("%s: no RabbitCT header", path);
+  RctHeader h;
+  memcpy(&h.width, raw, 4);
+  memcpy(&h.height, raw + 4, 4);
+  memcpy(&h.count, raw + 8, 4);
+  memcpy(h.hus, raw + 12, 8);
+  if (width)
+    *width = h.width;
+  if (height)
+    *height = h.height;
+  if (count)
+    *count = h.count;
+  if (hus) {
+    hus[0] = h.hus[0];
+    hus[1] = h.hus[1];
+  }
+  return 1;
+}
+
+int lolaCudaReconstructFile(const char *path, int problemSize, float voxelSize, float originIndex,
+    const LolaCudaConfig *config, float *h_volume, LolaCudaFileReport *report)
+{
+  if (path == NULL || h_volume == NULL)
+    return lolaSetError("reconstruct file: null argument");
+  const double t0 = nowSeconds();
+  uint32_t W, H, count;
+  float hus[2];
+  if (!lolaCudaReadRctHeader(path, &W, &H, &count, hus))
+    return 0;
+  if (W == 0 || H == 0 || count == 0)
+    return lolaSetError("%s: empty scan", path);
+  LolaCudaConfig c;
+  if (config != NULL)
+    c = *config;
+  else
+    lolaCudaDefaultConfig(&c);
+  LolaCudaGeometry g;
+  memset(&g, 0, sizeof(g));
+  g.problemSize = problemSize;
+  g.imageWidth = (int32_t)W;
+  g.imageHeight = (int32_t)H;
+  g.voxelSize = voxelSize;
+  g.originIndex = originIndex;
+  LolaCudaPlan *plan = NULL;
+  if (!lolaCudaPlanCreate(&g, &c, &plan))
+    return 0;
+
+  const int chunk = c.batch;
+  const size_t img = (size_t)W * H;
+  float *pinned[2] = { NULL, NULL };
+  double *mats = (double *)malloc((size_t)2 * chunk * 12 * sizeof(double));
+  FILE *f = fopen(path, "rb");
+  int ok = 1;
+  double readSeconds = 0.0;
+  if (mats == NULL || f == NULL) {
+    ok = lolaSetError("reconstruct file: cannot open %s or allocate", path);
+    goto done;
+  }
+  for (int i = 0; i < 2; ++i)
+    if (cudaHostAlloc((void **)&pinned[i], (size_t)chunk * img * sizeof(float),
+            cudaHostAllocDefault) != cudaSuccess) {
+      ok = lolaSetError("reconstruct file: pinned allocation failed");
+      goto done;
+    }
+  if (fseek(f, 20, SEEK_SET) != 0) {
+    ok = lolaSetError("%s: seek failed", path);
+    goto done;
+  }
+  if (!lolaCudaPlanUploadVolume(plan, h_volume)) {
+    ok = 0;
+    goto done;
+  }
+  for (uint32_t consumed = 0, k = 0; consumed < count; ++k) {
+    const int n = (count - consumed < (uint32_t)chunk) ? (int)(count - consumed) : chunk;
+    float *buf = pinned[k & 1];
+    double *m = mats + (size_t)(k & 1) * chunk * 12;
+    const double r0 = nowSeconds();
+    for (int i = 0; i < n; ++i) {
+      if (fread(m + 12 * (size_t)i, sizeof(double), 12, f) != 12 ||
+          fread(buf + (size_t)i * img, sizeof(float), img, f) != img) {
+        ok = lolaSetError("%s: truncated at projection %u", path, consumed + (uint32_t)i + 1);
+        goto done;
+      }
+    }
+    readSeconds += nowSeconds() - r0;
+    /* returns once the chunk is on the device; its pass runs on while the
+       next chunk is read into the other buffer */
+    if (!lolaCudaPlanBackprojectHost(plan, buf, img, m, n)) {
+      ok = 0;
+      goto done;
+    }
+    consumed += (uint32_t)n;
+  }
+  if (!lolaCudaPlanDownloadVolume(plan, h_volume))
+    ok = 0;
+done:
+  if (f != NULL)
+    fclose(f);
+  /* no page-locked buffer is released while a copy from it may be pending */
+  if (plan != NULL)
+    lolaCudaPlanSynchronize(plan);
+  for (int i = 0; i < 2; ++i)
+    if (pinned[i] != NULL)
+      cudaFreeHost(pinned[i]);
+  free(mats);
+  if (plan != NULL)
+    lolaCudaPlanDestroy(plan);
+  if (ok && report != NULL) {
+    report->seconds = nowSeconds() - t0;
+    report->readSeconds = readSeconds;
+    report->projections = count;
+    report->gups = (double)problemSize * problemSize * problemSize * count / report->seconds /
+                   1e9;
+    report->hus[0] = hus[0];
+    report->hus[1] = hus[1];
+  }
+  return ok;
+}

@@ -164,6 +164,23 @@ class Plan:
             pass
 
 
+def reconstruct_file(path, n: int, voxel_size: float, origin_index: float,
+                     volume: np.ndarray | None = None, cfg: LolaCudaConfig | None = None,
+                     **cfg_kw):
+    """lolaCudaReconstructFile: (volume, report dict)."""
+    from ._native import LolaCudaFileReport
+    lib = load_lolacuda()
+    vol = np.zeros((n, n, n), np.float32) if volume is None else volume
+    assert vol.dtype == np.float32 and vol.flags["C_CONTIGUOUS"] and vol.size == n ** 3
+    c = cfg if cfg is not None else config(**cfg_kw)
+    rep = LolaCudaFileReport()
+    check(lib.lolaCudaReconstructFile(str(path).encode(), n, voxel_size, origin_index,
+                                      C.byref(c), vol.ctypes.data, C.byref(rep)),
+          "reconstruct file")
+    return vol, {"seconds": rep.seconds, "read_seconds": rep.readSeconds,
+                 "projections": rep.projections, "gups": rep.gups, "hus": tuple(rep.hus)}
+
+
 def autotune(n: int, voxel_size: float, origin_index: float, width: int, height: int,
              d_images: int, matrices: np.ndarray, cfg: LolaCudaConfig | None = None,
              slab: tuple[int, int] | None = None, **cfg_kw):

@@ -277,3 +277,37 @@ def test_slabs_reassemble_unsharded_volume(lib):
             assert np.array_equal(joined, whole)
         else:
             assert metrics.errors(joined, whole)["rel_rmse"] < 1e-6
+
+
+@pytest.mark.parametrize("batch", [3, 16])
+def test_reconstruct_from_rct_file(lib, tmp_path, batch):
+    """lolaCudaReconstructFile on a .rct written with the reference's format:
+    same volume as the plan path, within the FP32 bar of the oracle."""
+    from rabbitct_gb300 import rct
+    from rabbitct_gb300.lolacuda import Plan, reconstruct_file
+    scan = synth.make_scan(small_spec(nproj=11, seed=71))
+    path = tmp_path / "scan.rct"
+    rct.write_rct(path, scan.images, scan.matrices, scan.hus)
+    n = 40
+    vs, o = _geom(n)
+    vol, rep = reconstruct_file(path, n, vs, o, batch=batch)
+    assert rep["projections"] == 11 and rep["hus"] == pytest.approx(scan.hus)
+    with Plan(n, vs, o, scan.width, scan.height, batch=batch) as plan:
+        plan.backproject_host(scan.images, scan.matrices)
+        want = plan.download()
+    assert np.array_equal(vol, want)
+    ref = oracle.bunny_f64(n, vs, o, scan.matrices, scan.images)
+    assert metrics.errors(vol, ref)["rel_rmse"] <= 1e-5
+
+
+def test_reconstruct_file_reports_truncation(lib, tmp_path):
+    from rabbitct_gb300 import rct
+    from rabbitct_gb300._native import LolaCudaError
+    from rabbitct_gb300.lolacuda import reconstruct_file
+    scan = synth.make_scan(small_spec(nproj=4, seed=72))
+    path = tmp_path / "cut.rct"
+    rct.write_rct(path, scan.images, scan.matrices, scan.hus)
+    data = path.read_bytes()
+    path.write_bytes(data[:len(data) - 1000])
+    with pytest.raises(LolaCudaError, match="truncated"):
+        reconstruct_file(path, 24, 256.0 / 24, synth.origin_index(24, 256.0 / 24))
