@@ -63,7 +63,9 @@ typedef struct {
 /* ---- 1. Module API --------------------------------------------------------
  * Replaces FncPrepareAlgorithmType (src/moduleLoader_types.h:10).  Called once
  * (src/rabbitRunner.c:222-232).  Allocates the device volume and the
- * projection ring and uploads the caller's volumeData as the starting volume. */
+ * projection ring and starts the upload of the caller's volumeData as the
+ * starting volume; the first pass overlaps that upload chunk by chunk, so
+ * volumeData must not change before finish (the runner does not touch it). */
 int lolaCudaPrepare(RabbitCtGlobalData *data);
 
 /* Replaces FncAlgorithmIterationType (src/moduleLoader_types.h:11).  Called
@@ -76,8 +78,9 @@ int lolaCudaPrepare(RabbitCtGlobalData *data);
 int lolaCudaBackprojection(RabbitCtGlobalData *data);
 
 /* Replaces FncFinishAlgorithmType (src/moduleLoader_types.h:12).  Flushes any
- * staged projections, copies the volume to data->volumeData and frees all
- * device resources (src/rabbitRunner.c:287). */
+ * staged projections, completes the copy of the volume to data->volumeData
+ * (which the scan's last pass starts chunk by chunk when the scan length is
+ * known) and frees all device resources (src/rabbitRunner.c:287). */
 int lolaCudaFinish(RabbitCtGlobalData *data);
 
 /* ---- 2. Configuration ------------------------------------------------------ */
@@ -171,6 +174,8 @@ typedef struct {
   int64_t tilePassesSkipped; /* ... whose footprint misses the detector */
   int64_t tilePassesStaged;  /* fast-path pairs served from shared-memory staging */
   int64_t stagedPasses;      /* passes launched with staging */
+  int64_t overlappedPasses;  /* passes run in z-chunks to overlap a volume transfer */
+  int64_t chunkLaunches;     /* kernel launches of those passes */
 } LolaCudaStats;
 
 typedef struct LolaCudaPlan LolaCudaPlan;
@@ -180,14 +185,29 @@ int lolaCudaPlanCreate(const LolaCudaGeometry *geometry, const LolaCudaConfig *c
     LolaCudaPlan **plan);
 int lolaCudaPlanDestroy(LolaCudaPlan *plan);
 
-/* Device pointer of the plan's FP32 volume, N x N x sliceCount, x fastest. */
+/* Device pointer of the plan's FP32 volume, N x N x sliceCount, x fastest.
+ * Work the caller then puts on the plan's stream is ordered after the plan's
+ * volume transfers. */
 float *lolaCudaPlanVolume(LolaCudaPlan *plan);
 /* cudaStream_t the plan launches on. */
 void *lolaCudaPlanStream(LolaCudaPlan *plan);
 
 int lolaCudaPlanZeroVolume(LolaCudaPlan *plan);
+/* Synchronous copies of the whole volume. */
 int lolaCudaPlanUploadVolume(LolaCudaPlan *plan, const float *h_volume);
 int lolaCudaPlanDownloadVolume(LolaCudaPlan *plan, float *h_volume);
+/* Starts the upload of h_volume in z-chunks on the plan's transfer stream and
+ * returns; the next pass starts on each chunk as soon as it has landed.
+ * h_volume must stay unchanged until lolaCudaPlanSynchronize (page-locked
+ * memory makes the call return at once). */
+int lolaCudaPlanUploadVolumeAsync(LolaCudaPlan *plan, const float *h_volume);
+/* Asks for the volume in h_volume after the next pass: that pass runs in
+ * z-chunks and each chunk is copied out as soon as it is finished, so the
+ * download overlaps the pass.  If no pass runs first, lolaCudaPlanSynchronize
+ * copies the volume as it is.  The copy is complete when
+ * lolaCudaPlanSynchronize returns.  Results are identical to a whole pass
+ * followed by lolaCudaPlanDownloadVolume. */
+int lolaCudaPlanStreamVolumeOut(LolaCudaPlan *plan, float *h_volume);
 
 /* Backprojects `count` FP32 projections that are already in device memory
  * (d_images[p * imageStride + j * W + i]) with host matrices

@@ -106,7 +106,9 @@ class LolaCudaStats(C.Structure):
                 ("tilePassesSlow", C.c_int64),
                 ("tilePassesSkipped", C.c_int64),
                 ("tilePassesStaged", C.c_int64),
-                ("stagedPasses", C.c_int64)]
+                ("stagedPasses", C.c_int64),
+                ("overlappedPasses", C.c_int64),
+                ("chunkLaunches", C.c_int64)]
 
 
 STORAGE = {"f32": 0, "f16": 1, "bf16": 2, "f32q": 3, "f16q": 4, "bf16q": 5, "tex32": 6,
@@ -132,6 +134,8 @@ _SIGNATURES = [
     ("lolaCudaPlanZeroVolume", C.c_int, [_P]),
     ("lolaCudaPlanUploadVolume", C.c_int, [_P, _P]),
     ("lolaCudaPlanDownloadVolume", C.c_int, [_P, _P]),
+    ("lolaCudaPlanUploadVolumeAsync", C.c_int, [_P, _P]),
+    ("lolaCudaPlanStreamVolumeOut", C.c_int, [_P, _P]),
     ("lolaCudaPlanBackprojectDevice", C.c_int, [_P, _P, C.c_size_t, _P, C.c_int]),
     ("lolaCudaPlanBackprojectHost", C.c_int, [_P, _P, C.c_size_t, _P, C.c_int]),
     ("lolaCudaPlanSynchronize", C.c_int, [_P]),

@@ -110,7 +110,8 @@ int lolaCudaReconstructFile(const char *path, int problemSize, float voxelSize, 
     ok = lolaSetError("%s: seek failed", path);
     goto done;
   }
-  if (!lolaCudaPlanUploadVolume(plan, h_volume)) {
+  /* the first pass overlaps the volume upload, the last one its download */
+  if (!lolaCudaPlanUploadVolumeAsync(plan, h_volume)) {
     ok = 0;
     goto done;
   }
@@ -127,6 +128,10 @@ int lolaCudaReconstructFile(const char *path, int problemSize, float voxelSize, 
       }
     }
     readSeconds += nowSeconds() - r0;
+    if (consumed + (uint32_t)n == count && !lolaCudaPlanStreamVolumeOut(plan, h_volume)) {
+      ok = 0;
+      goto done;
+    }
     /* returns once the chunk is on the device; its pass runs on while the
        next chunk is read into the other buffer */
     if (!lolaCudaPlanBackprojectHost(plan, buf, img, m, n)) {
@@ -135,7 +140,7 @@ int lolaCudaReconstructFile(const char *path, int problemSize, float voxelSize, 
     }
     consumed += (uint32_t)n;
   }
-  if (!lolaCudaPlanDownloadVolume(plan, h_volume))
+  if (!lolaCudaPlanSynchronize(plan))
     ok = 0;
 done:
   if (f != NULL)

@@ -188,6 +188,16 @@ struct LolaCudaPlan {
   LolaStageDesc stageDesc; /* tensor map of the ring for the current box */
   int stageBoxW, stageBoxH;
   size_t imageElems;
+  /* volume transfers overlapped with a pass: an asynchronous upload lands in
+     z-chunks and the next pass starts on each chunk as it arrives; a
+     streamed-out pass copies each chunk to the host once it is finished */
+  cudaStream_t xferStream;
+  cudaEvent_t upChunk[LOLA_XFER_CHUNKS], outChunk[LOLA_XFER_CHUNKS];
+  cudaEvent_t xferDone, streamMark;
+  int uploadChunks;  /* chunks of an asynchronous upload the next pass waits for */
+  int xferPending;   /* transfers the plan stream is not yet ordered after */
+  float *streamOut;  /* host target for the volume after the next pass */
+  float *outValid;   /* host copy streamed out after the last pass, if any */
   /* host-staged batch (module API / BackprojectHost) */
   int pending;
   double pendingMats[LOLA_MAX_BATCH][12];
@@ -237,6 +247,8 @@ static int planRelease(LolaCudaPlan *p)
     cudaStreamSynchronize(p->stream);
   if (p->copyStream)
     cudaStreamSynchronize(p->copyStream);
+  if (p->xferStream)
+    cudaStreamSynchronize(p->xferStream);
   for (int i = 0; i < p->nEvents; i++) {
     cudaEventDestroy(p->events[i].start);
     cudaEventDestroy(p->events[i].stop);
@@ -262,6 +274,18 @@ static int planRelease(LolaCudaPlan *p)
     cudaStreamDestroy(p->stream);
   if (p->copyStream)
     cudaStreamDestroy(p->copyStream);
+  for (int i = 0; i < LOLA_XFER_CHUNKS; i++) {
+    if (p->upChunk[i])
+      cudaEventDestroy(p->upChunk[i]);
+    if (p->outChunk[i])
+      cudaEventDestroy(p->outChunk[i]);
+  }
+  if (p->xferDone)
+    cudaEventDestroy(p->xferDone);
+  if (p->streamMark)
+    cudaEventDestroy(p->streamMark);
+  if (p->xferStream)
+    cudaStreamDestroy(p->xferStream);
   free(p);
   return 1;
 }
@@ -281,6 +305,13 @@ static int planInit(LolaCudaPlan *p)
   CUDA_TRY(cudaEventCreateWithFlags(&p->stageReady, cudaEventDisableTiming));
   CUDA_TRY(cudaEventCreate(&p->timerStart));
   CUDA_TRY(cudaEventCreate(&p->timerStop));
+  CUDA_TRY(cudaStreamCreateWithFlags(&p->xferStream, cudaStreamNonBlocking));
+  for (int i = 0; i < LOLA_XFER_CHUNKS; i++) {
+    CUDA_TRY(cudaEventCreateWithFlags(&p->upChunk[i], cudaEventDisableTiming));
+    CUDA_TRY(cudaEventCreateWithFlags(&p->outChunk[i], cudaEventDisableTiming));
+  }
+  CUDA_TRY(cudaEventCreateWithFlags(&p->xferDone, cudaEventDisableTiming));
+  CUDA_TRY(cudaEventCreateWithFlags(&p->streamMark, cudaEventDisableTiming));
 
   LolaStoreDesc *s = &p->store;
   s->storage = p->cfg.storage;
@@ -384,9 +415,24 @@ int lolaCudaPlanCreate(const LolaCudaGeometry *g, const LolaCudaConfig *cfg, Lol
   return 1;
 }
 
+/* Orders the plan stream after every volume transfer issued so far. */
+static int joinTransfers(LolaCudaPlan *p)
+{
+  if (p->xferPending) {
+    CUDA_TRY(cudaStreamWaitEvent(p->stream, p->xferDone, 0));
+    p->xferPending = 0;
+  }
+  p->uploadChunks = 0;
+  return 1;
+}
+
 float *lolaCudaPlanVolume(LolaCudaPlan *p)
 {
-  return p ? p->d_volume : NULL;
+  if (p == NULL)
+    return NULL;
+  cudaSetDevice(p->device);
+  joinTransfers(p);
+  return p->d_volume;
 }
 
 void *lolaCudaPlanStream(LolaCudaPlan *p)
@@ -403,6 +449,32 @@ size_t lolaPlanVoxels(const LolaCudaPlan *p)
 static size_t volumeBytes(const LolaCudaPlan *p)
 {
   return lolaPlanVoxels(p) * sizeof(float);
+}
+
+/* Number of z-chunks a volume transfer is split into; chunk boundaries fall
+   on tile boundaries (multiples of voxelsPerThread from the slab start), so a
+   pass launched chunk by chunk computes exactly the tiles of a whole pass. */
+static int xferChunks(const LolaCudaPlan *p)
+{
+  const int vpt = p->cfg.voxelsPerThread;
+  const int tiles = (p->geom.sliceCount + vpt - 1) / vpt;
+  size_t k = volumeBytes(p) / LOLA_XFER_MIN_CHUNK_BYTES;
+  if (k > LOLA_XFER_CHUNKS)
+    k = LOLA_XFER_CHUNKS;
+  if (k > (size_t)tiles)
+    k = (size_t)tiles;
+  return k < 1 ? 1 : (int)k;
+}
+
+/* Slices [*zb, *ze) of chunk c of k, relative to the slab start. */
+static void xferChunkRange(const LolaCudaPlan *p, int c, int k, int *zb, int *ze)
+{
+  const int vpt = p->cfg.voxelsPerThread;
+  const int nz = p->geom.sliceCount;
+  const int tiles = (nz + vpt - 1) / vpt;
+  *zb = (int)((long long)tiles * c / k) * vpt;
+  const int e = (int)((long long)tiles * (c + 1) / k) * vpt;
+  *ze = e > nz ? nz : e;
 }
 
 int lolaCudaSlab(int N, int rank, int ranks, int align, int32_t *begin, int32_t *count)
@@ -424,7 +496,10 @@ int lolaCudaPlanZeroVolume(LolaCudaPlan *p)
   if (p == NULL)
     return setError("null plan");
   CUDA_TRY(cudaSetDevice(p->device));
+  if (!joinTransfers(p))
+    return 0;
   CUDA_TRY(cudaMemsetAsync(p->d_volume, 0, volumeBytes(p), p->stream));
+  p->outValid = NULL;
   return 1;
 }
 
@@ -433,8 +508,44 @@ int lolaCudaPlanUploadVolume(LolaCudaPlan *p, const float *h)
   if (p == NULL || h == NULL)
     return setError("null argument");
   CUDA_TRY(cudaSetDevice(p->device));
+  if (!joinTransfers(p))
+    return 0;
   CUDA_TRY(cudaMemcpyAsync(p->d_volume, h, volumeBytes(p), cudaMemcpyHostToDevice, p->stream));
   CUDA_TRY(cudaStreamSynchronize(p->stream));
+  p->outValid = NULL;
+  return 1;
+}
+
+int lolaCudaPlanUploadVolumeAsync(LolaCudaPlan *p, const float *h)
+{
+  if (p == NULL || h == NULL)
+    return setError("null argument");
+  CUDA_TRY(cudaSetDevice(p->device));
+  /* the upload overwrites what earlier work on the plan stream produces */
+  CUDA_TRY(cudaEventRecord(p->streamMark, p->stream));
+  CUDA_TRY(cudaStreamWaitEvent(p->xferStream, p->streamMark, 0));
+  const int k = xferChunks(p);
+  const size_t slice = (size_t)p->geom.problemSize * (size_t)p->geom.problemSize;
+  for (int c = 0; c < k; c++) {
+    int zb, ze;
+    xferChunkRange(p, c, k, &zb, &ze);
+    if (ze > zb)
+      CUDA_TRY(cudaMemcpyAsync(p->d_volume + (size_t)zb * slice, h + (size_t)zb * slice,
+          (size_t)(ze - zb) * slice * sizeof(float), cudaMemcpyHostToDevice, p->xferStream));
+    CUDA_TRY(cudaEventRecord(p->upChunk[c], p->xferStream));
+  }
+  CUDA_TRY(cudaEventRecord(p->xferDone, p->xferStream));
+  p->xferPending = 1;
+  p->uploadChunks = k;
+  p->outValid = NULL;
+  return 1;
+}
+
+int lolaCudaPlanStreamVolumeOut(LolaCudaPlan *p, float *h)
+{
+  if (p == NULL || h == NULL)
+    return setError("null argument");
+  p->streamOut = h;
   return 1;
 }
 
@@ -443,6 +554,8 @@ int lolaCudaPlanDownloadVolume(LolaCudaPlan *p, float *h)
   if (p == NULL || h == NULL)
     return setError("null argument");
   CUDA_TRY(cudaSetDevice(p->device));
+  if (!joinTransfers(p))
+    return 0;
   CUDA_TRY(cudaMemcpyAsync(h, p->d_volume, volumeBytes(p), cudaMemcpyDeviceToHost, p->stream));
   CUDA_TRY(cudaStreamSynchronize(p->stream));
   return 1;
@@ -675,8 +788,55 @@ static int launchPass(LolaCudaPlan *p, const double *mats, int count)
     CUDA_TRY(cudaEventRecord(ev->start, p->stream));
   }
   const int staged = prepareStage(p, mats, count);
-  LAUNCH_TRY(lolaLaunchBackproject(&p->store, &P, staged ? &p->stageDesc : NULL, p->d_ring,
-      p->d_volume, p->cfg.collectStats ? p->d_counters : NULL, p->stream));
+  const LolaStageDesc *sd = staged ? &p->stageDesc : NULL;
+  unsigned long long *counters = p->cfg.collectStats ? p->d_counters : NULL;
+  const int up = p->uploadChunks > 0, out = p->streamOut != NULL;
+  if (!up && !out) {
+    if (!joinTransfers(p))
+      return 0;
+    LAUNCH_TRY(lolaLaunchBackproject(&p->store, &P, sd, p->d_ring, p->d_volume, counters,
+        p->stream));
+    p->outValid = NULL;
+  } else {
+    /* chunk by chunk: each starts once its slices have landed and/or is
+       copied out as soon as it is done; tiles are those of a whole pass */
+    if (!up && !joinTransfers(p))
+      return 0;
+    const int k = up ? p->uploadChunks : xferChunks(p);
+    const size_t slice = (size_t)P.N * (size_t)P.N;
+    for (int c = 0; c < k; c++) {
+      int zb, ze;
+      xferChunkRange(p, c, k, &zb, &ze);
+      if (up)
+        CUDA_TRY(cudaStreamWaitEvent(p->stream, p->upChunk[c], 0));
+      if (ze <= zb)
+        continue;
+      LolaPassParams Pc = P;
+      Pc.zBegin = P.zBegin + zb;
+      Pc.zEnd = P.zBegin + ze;
+      LAUNCH_TRY(lolaLaunchBackproject(&p->store, &Pc, sd, p->d_ring,
+          p->d_volume + (size_t)zb * slice, counters, p->stream));
+      p->stats.chunkLaunches++;
+      if (out) {
+        CUDA_TRY(cudaEventRecord(p->outChunk[c], p->stream));
+        CUDA_TRY(cudaStreamWaitEvent(p->xferStream, p->outChunk[c], 0));
+        CUDA_TRY(cudaMemcpyAsync(p->streamOut + (size_t)zb * slice,
+            p->d_volume + (size_t)zb * slice, (size_t)(ze - zb) * slice * sizeof(float),
+            cudaMemcpyDeviceToHost, p->xferStream));
+      }
+    }
+    p->stats.overlappedPasses++;
+    /* the plan stream has waited for every uploaded chunk */
+    p->uploadChunks = 0;
+    p->xferPending = 0;
+    p->outValid = NULL;
+    if (out) {
+      CUDA_TRY(cudaEventRecord(p->xferDone, p->xferStream));
+      p->xferPending = 1;
+      p->outValid = p->streamOut;
+      p->streamOut = NULL;
+    }
+  }
   if (staged) {
     p->stagedLaunched = 1;
     p->stats.stagedPasses++;
@@ -780,8 +940,20 @@ int lolaCudaPlanSynchronize(LolaCudaPlan *p)
   CUDA_TRY(cudaSetDevice(p->device));
   if (!flushPending(p))
     return 0;
+  if (p->streamOut != NULL) {
+    /* no pass consumed the stream-out request: copy the volume as it is */
+    if (!joinTransfers(p))
+      return 0;
+    CUDA_TRY(cudaMemcpyAsync(p->streamOut, p->d_volume, volumeBytes(p), cudaMemcpyDeviceToHost,
+        p->stream));
+    p->outValid = p->streamOut;
+    p->streamOut = NULL;
+  }
   CUDA_TRY(cudaStreamSynchronize(p->copyStream));
+  CUDA_TRY(cudaStreamSynchronize(p->xferStream));
   CUDA_TRY(cudaStreamSynchronize(p->stream));
+  p->xferPending = 0;
+  p->uploadChunks = 0;
   return checkStageError(p);
 }
 
@@ -936,6 +1108,7 @@ int lolaCudaDeviceSynchronize(void)
 
 static LolaCudaPlan *gPlan = NULL;
 static uint32_t gTotalProjections = 0; /* known with -a (src/rabbitRunner.c:209-210) */
+static int gVolumePinned = 0;          /* volumeData is page-locked host memory */
 
 static int moduleFail(const char *where)
 {
@@ -975,10 +1148,16 @@ int lolaCudaPrepare(RabbitCtGlobalData *d)
   if (!lolaCudaPlanCreate(&g, &c, &gPlan))
     return moduleFail("prepare");
   /* the module accumulates into whatever the caller's volume holds, like
-     LolaBunny's `+=` (src/LolaBunny.c:68) */
-  if (!lolaCudaPlanUploadVolume(gPlan, d->volumeData))
+     LolaBunny's `+=` (src/LolaBunny.c:68); the upload runs on while the first
+     batch is staged, and the first pass starts on each z-chunk as it lands
+     (the runner leaves volumeData alone until finish) */
+  if (!lolaCudaPlanUploadVolumeAsync(gPlan, d->volumeData))
     return moduleFail("prepare");
   gTotalProjections = d->numberOfProjections;
+  struct cudaPointerAttributes attr;
+  gVolumePinned = cudaPointerGetAttributes(&attr, d->volumeData) == cudaSuccess &&
+                  attr.type == cudaMemoryTypeHost;
+  cudaGetLastError(); /* an unknown pointer is not an error here */
   return 1;
 }
 
@@ -1010,11 +1189,18 @@ int lolaCudaBackprojection(RabbitCtGlobalData *d)
       setError("projection %u has no image or matrix", i);
       return moduleFail("backprojection");
     }
+    const int last = gTotalProjections > 0 && pr->id >= (int)gTotalProjections;
+    /* the scan's last pass copies the volume out chunk by chunk as it
+       finishes them, overlapping the download with the pass's tail; only
+       into page-locked memory, where the copies do not hold up this (timed)
+       call — a pageable volume is copied in the untimed finish as before */
+    if (last && gVolumePinned && !lolaCudaPlanStreamVolumeOut(p, d->volumeData))
+      return moduleFail("backprojection");
     if (!stageHost(p, pr->image, pr->matrix, &flushed))
       return moduleFail("backprojection");
     /* the last view of the scan closes the pass, so no work is left for the
        untimed finish (src/rabbitRunner.c:287) */
-    if (gTotalProjections > 0 && pr->id >= (int)gTotalProjections && p->pending > 0) {
+    if (last && p->pending > 0) {
       if (!flushPending(p))
         return moduleFail("backprojection");
       flushed = 1;
@@ -1047,7 +1233,15 @@ int lolaCudaFinish(RabbitCtGlobalData *d)
     setError("volumeData is null");
     return moduleFail("finish");
   }
-  if (!lolaCudaPlanSynchronize(gPlan) || !lolaCudaPlanDownloadVolume(gPlan, d->volumeData))
+  LolaCudaPlan *p = gPlan;
+  /* unless the last pass already streamed the volume out, the closing pass
+     (or, with none pending, a plain copy) delivers it */
+  if ((p->pending > 0 || p->outValid != d->volumeData) &&
+      !lolaCudaPlanStreamVolumeOut(p, d->volumeData))
+    return moduleFail("finish");
+  if (!lolaCudaPlanSynchronize(p))
+    return moduleFail("finish");
+  if (p->outValid != d->volumeData && !lolaCudaPlanDownloadVolume(p, d->volumeData))
     return moduleFail("finish");
   planRelease(gPlan);
   gPlan = NULL;

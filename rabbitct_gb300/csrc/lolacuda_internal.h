@@ -66,6 +66,12 @@ typedef struct {
 /* Stage buffers of the staged pass (a build-time tuning knob). */
 #ifndef LOLA_STAGES
 #define LOLA_STAGES 3
+
+/* z-chunks of a volume transfer overlapped with a pass (upload before the
+   first pass, download after the last one) */
+#define LOLA_XFER_CHUNKS 8
+/* volumes smaller than this move in one piece */
+#define LOLA_XFER_MIN_CHUNK_BYTES (32u << 20)
 #endif
 
 /* Shared-memory staging of one pass (bp_staged.cuh): the tensor map over the

@@ -71,6 +71,7 @@ class Plan:
         g = LolaCudaGeometry(self.n, self.width, self.height, voxel_size, origin_index,
                              self.slab[0], self.slab[1])
         self.cfg = cfg if cfg is not None else config(**cfg_kw)
+        self._hold: list[np.ndarray] = []  # host buffers of transfers in flight
         h = C.c_void_p()
         check(self.lib.lolaCudaPlanCreate(C.byref(g), C.byref(self.cfg), C.byref(h)),
               "plan create")
@@ -91,6 +92,24 @@ class Plan:
         vol = np.ascontiguousarray(vol, np.float32)
         assert vol.size == self.n * self.n * self.slab[1]
         check(self.lib.lolaCudaPlanUploadVolume(self.handle, vol.ctypes.data), "upload volume")
+
+    def upload_async(self, vol: np.ndarray) -> None:
+        """Starts a chunked upload that the next pass overlaps; `vol` is kept
+        alive (and must stay unchanged) until synchronize()."""
+        assert vol.dtype == np.float32 and vol.flags.c_contiguous
+        assert vol.size == self.n * self.n * self.slab[1]
+        self._hold.append(vol)
+        check(self.lib.lolaCudaPlanUploadVolumeAsync(self.handle, vol.ctypes.data),
+              "upload volume async")
+
+    def stream_out(self, out: np.ndarray) -> np.ndarray:
+        """The volume lands in `out` after the next pass (or at synchronize()),
+        chunk by chunk as the pass finishes; complete after synchronize()."""
+        assert out.dtype == np.float32 and out.flags.c_contiguous
+        assert out.size == self.n * self.n * self.slab[1]
+        self._hold.append(out)
+        check(self.lib.lolaCudaPlanStreamVolumeOut(self.handle, out.ctypes.data), "stream out")
+        return out
 
     def download(self, out: np.ndarray | None = None) -> np.ndarray:
         """The plan's volume (its slab: sliceCount x N x N), z slowest."""
@@ -116,6 +135,7 @@ class Plan:
 
     def synchronize(self) -> None:
         check(self.lib.lolaCudaPlanSynchronize(self.handle), "synchronize")
+        self._hold.clear()
 
     def timer_start(self) -> None:
         check(self.lib.lolaCudaPlanTimerStart(self.handle), "timer start")
@@ -148,8 +168,9 @@ class Plan:
 
     def close(self) -> None:
         if getattr(self, "handle", None):
-            self.lib.lolaCudaPlanDestroy(self.handle)
+            self.lib.lolaCudaPlanDestroy(self.handle)  # waits for its streams
             self.handle = None
+            self._hold.clear()
 
     def __enter__(self):
         return self
