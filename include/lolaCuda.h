@@ -286,6 +286,19 @@ int lolaCudaVerifyVolume(float *d_volume, size_t voxels, const uint16_t *h_refer
 int lolaCudaPlanVerify(LolaCudaPlan *plan, const uint16_t *h_reference, const float *hus,
     int convertInPlace, LolaCudaQuality *quality);
 
+/* The runner's optional outputs from the plan's volume, copying only slice
+ * N/2-1 to the host.  lolaCudaPlanWriteSlicePgm replaces the -p writer
+ * (src/rabbitRunner.c:289-315): the slice in HU as a 16-bit big-endian PGM;
+ * call it before lolaCudaPlanWriteResult, which converts the volume to HU.
+ * lolaCudaPlanWriteResult replaces the -c result.rctd writer
+ * (src/rabbitRunner.c:317-412): verifies on the device (converting in place,
+ * as the runner does), then writes the file with totalMicroseconds /
+ * numberOfImages as every image's time.  It needs a whole-volume plan. */
+int lolaCudaPlanWriteSlicePgm(LolaCudaPlan *plan, const char *path, const float *hus);
+int lolaCudaPlanWriteResult(LolaCudaPlan *plan, const char *path, const uint16_t *h_reference,
+    const float *hus, uint32_t numberOfImages, uint64_t totalMicroseconds,
+    LolaCudaQuality *quality);
+
 /* ---- Geometry analysis on the device ----------------------------------------
  * Replaces computeLineRanges (src/analyseGeometry.c:102-298) for the
  * reference's clipping modules: range[view] (view < data->numberOfProjections,

@@ -157,6 +157,9 @@ _SIGNATURES = [
     ("lolaCudaVerifyVolume", C.c_int, [_P, C.c_size_t, _P, _P, C.c_int, _P,
                                        C.POINTER(LolaCudaQuality)]),
     ("lolaCudaPlanVerify", C.c_int, [_P, _P, _P, C.c_int, C.POINTER(LolaCudaQuality)]),
+    ("lolaCudaPlanWriteSlicePgm", C.c_int, [_P, C.c_char_p, _P]),
+    ("lolaCudaPlanWriteResult", C.c_int, [_P, C.c_char_p, _P, _P, C.c_uint32, C.c_uint64,
+                                          C.POINTER(LolaCudaQuality)]),
     ("lolaCudaSlab", C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int32),
                                C.POINTER(C.c_int32)]),
     ("lolaCudaBatchCreate", C.c_int, [_P, C.c_int, C.POINTER(LolaCudaConfig), C.POINTER(_P)]),

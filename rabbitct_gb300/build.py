@@ -29,7 +29,7 @@ CU_SOURCES = [
     "lolacuda_dispatch.cu", "lolacuda_probe.cu", "lolacuda_noalloc.cu",
     "lolacuda_geometry.cu", "lolacuda_verify.cu", "lolacuda_batch.cu",
 ]
-C_SOURCES = ["lolacuda_host.c", "lolacuda_file.c"]
+C_SOURCES = ["lolacuda_host.c", "lolacuda_file.c", "lolacuda_result.c"]
 
 
 def _cuda_home() -> Path:
@@ -95,7 +95,9 @@ def build_lolacuda(force: bool = False, jobs: int | None = None) -> Path:
         src = CSRC / name
         obj = OBJ / (name + ".o")
         if force or _stale(obj, [src] + headers):
-            _run(["gcc", "-O2", "-std=c99", "-fPIC", "-Wall", "-Wextra", "-Wno-unused-parameter",
+            # no contraction: host arithmetic rounds alike on x86 and Arm
+            _run(["gcc", "-O2", "-std=c99", "-fPIC", "-ffp-contract=off", "-Wall", "-Wextra",
+                  "-Wno-unused-parameter",
                   *defines, *common_inc, "-I" + str(cuda / "include"), "-c", str(src), "-o",
                   str(obj)])
         return obj

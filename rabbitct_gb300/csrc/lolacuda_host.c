@@ -446,6 +446,11 @@ size_t lolaPlanVoxels(const LolaCudaPlan *p)
   return n * n * (size_t)p->geom.sliceCount;
 }
 
+const LolaCudaGeometry *lolaPlanGeometry(const LolaCudaPlan *p)
+{
+  return &p->geom;
+}
+
 static size_t volumeBytes(const LolaCudaPlan *p)
 {
   return lolaPlanVoxels(p) * sizeof(float);

@@ -121,6 +121,7 @@ int lolaLaunchBackproject(const LolaStoreDesc *store, const LolaPassParams *para
 
 /* Voxels of a plan's volume (N^3). */
 size_t lolaPlanVoxels(const LolaCudaPlan *plan);
+const LolaCudaGeometry *lolaPlanGeometry(const LolaCudaPlan *p);
 
 /* Sets the thread's lolaCudaLastError() message; returns 0. */
 int lolaSetError(const char *fmt, ...);

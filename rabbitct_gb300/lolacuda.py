@@ -6,6 +6,7 @@ is no Python or CPU implementation of the backprojection in this package.
 from __future__ import annotations
 
 import ctypes as C
+import os
 
 import numpy as np
 
@@ -155,6 +156,26 @@ class Plan:
         q = LolaCudaQuality()
         check(self.lib.lolaCudaPlanVerify(self.handle, ref.ctypes.data, h.ctypes.data,
                                           int(convert_in_place), C.byref(q)), "verify")
+        return {"rmse_hu": q.rmse, "mse_hu2": q.mse, "max_abs_hu": q.maxAbs,
+                "psnr_db": q.psnr, "histogram": list(q.histogram)}
+
+    def write_pgm(self, path, hus) -> None:
+        """The runner's -p slice (N/2-1, HU, 16-bit PGM) from the device volume."""
+        h = np.asarray(hus, np.float32)
+        check(self.lib.lolaCudaPlanWriteSlicePgm(self.handle, os.fsencode(path), h.ctypes.data),
+              "write pgm")
+
+    def write_result(self, path, reference_hu: np.ndarray, hus, number_of_images: int,
+                     total_usec: int) -> dict:
+        """The runner's -c result.rctd; converts the device volume to HU."""
+        from ._native import LolaCudaQuality
+        ref = np.ascontiguousarray(reference_hu, np.uint16)
+        assert ref.size == self.n ** 3
+        h = np.asarray(hus, np.float32)
+        q = LolaCudaQuality()
+        check(self.lib.lolaCudaPlanWriteResult(self.handle, os.fsencode(path), ref.ctypes.data,
+                                               h.ctypes.data, int(number_of_images),
+                                               int(total_usec), C.byref(q)), "write result")
         return {"rmse_hu": q.rmse, "mse_hu2": q.mse, "max_abs_hu": q.maxAbs,
                 "psnr_db": q.psnr, "histogram": list(q.histogram)}
 

@@ -7,7 +7,8 @@ it builds the unmodified reference into oracle/_ref (oracle/ref.mk) and runs
     src/LolaOPT.c), driven like src/rabbitRunner.c drives them;
   - computeLineRanges and computeShadowOfProjection (src/analyseGeometry.c);
   - the reference runner binary end to end on a .rct file (N=128, the
-    runner's smallest size), including its -c verification printout.
+    runner's smallest size), including its -c verification printout, its
+    result.rctd file and its -p PGM slice.
 
 Outputs (committed): tests/golden/*.npz and runner_n128.json.  Inputs are
 synthetic scans from rabbitct_gb300.synth; small cases store the images
@@ -109,10 +110,25 @@ def runner_case(tmp):
     refvol = os.path.join(tmp, "ref.vol")
     hu_ref.tofile(refvol)
     env = dict(os.environ, OMP_NUM_THREADS="4")
+    pgm = os.path.join(tmp, "slice.pgm")
     proc = subprocess.run([str(oracle.REF_RUNNER), "-m", "LolaBunny", "-s", str(n), "-b", "2",
-                           "-i", path, "-o", out, "-c", refvol], capture_output=True,
+                           "-i", path, "-o", out, "-c", refvol, "-p", pgm], capture_output=True,
                           text=True, cwd=tmp, env=env, check=True)
     vol = np.fromfile(out, np.float32).reshape(n, n, n)
+    # the runner's optional outputs: -p slice (written from the FP32 volume)
+    # and result.rctd (written by -c into the working directory); the raw
+    # middle slice they come from needs a second run without -c (LolaBunny is
+    # deterministic), because -c converts the volume to HU before -o
+    raw_out = os.path.join(tmp, "bunny_raw.vol")
+    subprocess.run([str(oracle.REF_RUNNER), "-m", "LolaBunny", "-s", str(n), "-b", "2",
+                    "-i", path, "-o", raw_out], capture_output=True, text=True, cwd=tmp,
+                   env=env, check=True)
+    raw = np.fromfile(raw_out, np.float32).reshape(n, n, n)
+    rctd = np.fromfile(os.path.join(tmp, "result.rctd"), np.uint8)
+    np.savez_compressed(HERE / "runner_n128_outputs.npz",
+                        raw_mid_slice=raw[n // 2 - 1].copy(),
+                        pgm=np.fromfile(pgm, np.uint8), rctd=rctd,
+                        hu_mid_slice=vol[n // 2 - 1].copy())
     def grab(pat):
         m = re.search(pat, proc.stdout)
         return float(m.group(1)) if m else None

@@ -311,3 +311,41 @@ def test_reconstruct_file_reports_truncation(lib, tmp_path):
     path.write_bytes(data[:len(data) - 1000])
     with pytest.raises(LolaCudaError, match="truncated"):
         reconstruct_file(path, 24, 256.0 / 24, synth.origin_index(24, 256.0 / 24))
+
+
+def test_runner_output_writers_match_reference_files(lib, tmp_path):
+    """lolaCudaPlanWriteSlicePgm / lolaCudaPlanWriteResult on a volume whose
+    middle slice is the reference runner's raw slice: the PGM equals the
+    runner's file byte for byte, result.rctd has its layout and HU slice, and
+    its metrics equal the restatement over the whole volume."""
+    import json
+    from pathlib import Path
+
+    from rabbitct_gb300.lolacuda import Plan
+    golden = Path(__file__).resolve().parent / "golden"
+    info = json.loads((golden / "runner_n128.json").read_text())
+    z = np.load(golden / "runner_n128_outputs.npz")
+    n, hus = info["n"], info["hus"]
+    rng = np.random.default_rng(17)
+    vol = rng.uniform(-0.002, float(z["raw_mid_slice"].max()), (n, n, n)).astype(np.float32)
+    vol[n // 2 - 1] = z["raw_mid_slice"]
+    hu_ref = metrics.to_hu(vol, hus) + rng.integers(-12, 13, vol.shape)
+    hu_ref = np.clip(hu_ref, 0, 4095).astype(np.uint16)
+    vs, o = _geom(n)
+    with Plan(n, vs, o, 64, 48) as plan:
+        plan.upload(vol)
+        plan.write_pgm(tmp_path / "slice.pgm", hus)
+        q = plan.write_result(tmp_path / "result.rctd", hu_ref, hus, 4, 4 * 19437 + 3)
+    assert (tmp_path / "slice.pgm").read_bytes() == z["pgm"].tobytes()
+    got, ref = (tmp_path / "result.rctd").read_bytes(), z["rctd"].tobytes()
+    assert len(got) == len(ref)
+    assert got[:12] == ref[:12]                                   # magic, size, images
+    assert got[12:44] == np.full(4, 19437, np.uint64).tobytes()   # mean time per image
+    assert got[44:44 + 4 * n * n] == ref[44:44 + 4 * n * n]       # HU slice
+    assert got[-4:] == ref[-4:]
+    want = metrics.hu_quality(vol, hu_ref, hus)
+    off = 44 + 4 * n * n
+    mse, mx = np.frombuffer(got[off:off + 16], np.float64)
+    hist = np.frombuffer(got[off + 16:off + 60], np.uint32)
+    assert mse == want["mse_hu2"] and mx == want["max_abs_hu"]    # integer sums: exact
+    assert hist.tolist() == want["histogram"] == q["histogram"]

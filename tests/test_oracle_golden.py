@@ -183,3 +183,41 @@ def test_live_reference_runner_reads_our_rct(tmp_path):
     v = np.fromfile(out, np.float32).reshape(128, 128, 128)
     np.testing.assert_array_max_ulp(v, oracle.bunny_f32(128, vs, o, scan.matrices, scan.images),
                                     maxulp=2)
+
+
+def _parse_rctd(raw: bytes, n: int) -> dict:
+    """result.rctd as the reference runner writes it (src/rabbitRunner.c:396-404)."""
+    head = np.frombuffer(raw[:12], np.int32)
+    k = int(head[2])
+    off = 12 + 8 * k
+    out = {"magic": int(head[0]), "size": int(head[1]), "images": k,
+           "runtime": np.frombuffer(raw[12:off], np.uint64),
+           "slice": np.frombuffer(raw[off:off + 4 * n * n], np.float32).reshape(n, n)}
+    off += 4 * n * n
+    out["mse"], out["max"] = np.frombuffer(raw[off:off + 16], np.float64)
+    out["hist"] = np.frombuffer(raw[off + 16:off + 60], np.uint32)
+    out["magic_end"] = int(np.frombuffer(raw[off + 60:off + 64], np.int32)[0])
+    assert len(raw) == off + 64
+    return out
+
+
+def test_runner_output_files_follow_hu_restatement():
+    """The reference runner's -p PGM and result.rctd for the N=128 run: both
+    slices are metrics.to_hu of the raw FP32 middle slice (the HU formula the
+    device writers use), and the file's metrics are the ones it printed."""
+    info = json.loads((GOLDEN / "runner_n128.json").read_text())
+    z = np.load(GOLDEN / "runner_n128_outputs.npz")
+    n = info["n"]
+    hu = metrics.to_hu(z["raw_mid_slice"], info["hus"])
+    pgm = z["pgm"].tobytes()
+    head = f"P5\n{n} {n}\n4095\n".encode()
+    assert pgm.startswith(head)
+    assert np.array_equal(np.frombuffer(pgm[len(head):], ">u2").reshape(n, n), hu)
+    r = _parse_rctd(z["rctd"].tobytes(), n)
+    assert (r["magic"], r["size"], r["images"], r["magic_end"]) == (591984, n, 4, 489195)
+    assert np.array_equal(r["slice"], hu)
+    assert np.array_equal(r["slice"], z["hu_mid_slice"])
+    printed = info["runner_quality"]
+    assert r["mse"] == pytest.approx(printed["mse_hu2"], rel=1e-5)
+    assert r["max"] == printed["max_abs_hu"]
+    assert int(r["hist"].sum()) == n ** 3
