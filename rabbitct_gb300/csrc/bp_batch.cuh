@@ -105,14 +105,14 @@ __global__ void __launch_bounds__(256, LOLA_BATCH_MIN_BLOCKS) batchPassKernel(co
       const int x = x0 + threadIdx.x, y = y0 + threadIdx.y;
       const bool inXY = (x < N) && (y < N);
       const size_t slice = (size_t)N * (size_t)N;
-      float acc[VPT], comp[VPT];
+      float2 acc[VPT / 2], comp[VPT / 2];
       {
         const float *vcol = J.volume + ((size_t)z0 * N + (size_t)(inXY ? y : 0)) * (size_t)N +
                             (inXY ? x : 0);
 #pragma unroll
         for (int k = 0; k < VPT; ++k) {
-          acc[k] = (inXY && z0 + k < N) ? vcol[k * slice] : 0.0f;
-          comp[k] = 0.0f;
+          voxel(acc, k) = (inXY && z0 + k < N) ? vcol[k * slice] : 0.0f;
+          voxel(comp, k) = 0.0f;
         }
       }
       /* read through a volatile view: re-read per projection from shared
@@ -132,7 +132,9 @@ __global__ void __launch_bounds__(256, LOLA_BATCH_MIN_BLOCKS) batchPassKernel(co
         const void *img = Jv->ring + (size_t)tp.slot * Jv->slotBytes;
         const unsigned long long tex =
             (Layout<S>::kTex || Layout<S>::kMixed) ? Jv->tex[tp.slot] : 0ull;
-        if (mode == MODE_FAST)
+        if (mode == MODE_FAST && tp.pos && LOLA_PAIRED)
+          applyPairs<S, VPT, KAHAN>(tp, img, tex, a, fi, fj, acc, comp);
+        else if (mode == MODE_FAST)
           applyProjection<S, VPT, KAHAN, false>(tp, img, tex, a, fi, fj, acc, comp);
         else
           applyProjection<S, VPT, KAHAN, true>(tp, img, tex, a, fi, fj, acc, comp);
@@ -142,7 +144,7 @@ __global__ void __launch_bounds__(256, LOLA_BATCH_MIN_BLOCKS) batchPassKernel(co
 #pragma unroll
       for (int k = 0; k < VPT; ++k)
         if (inXY && z0 + k < N)
-          vcol[k * slice] = KAHAN ? (acc[k] - comp[k]) : acc[k];
+          vcol[k * slice] = KAHAN ? (voxel(acc, k) - voxel(comp, k)) : voxel(acc, k);
     }
     __syncthreads(); /* J, sp[] and the item fields are rewritten next */
   }

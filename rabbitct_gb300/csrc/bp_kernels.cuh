@@ -45,18 +45,27 @@ namespace lola {
 
 enum { MODE_SKIP = 0, MODE_FAST = 1, MODE_SLOW = 2 };
 
+/* 1: positive fast tiles take the packed two-voxel path (applyPairs); 0: every
+   tile the one-voxel path (a build-time switch for comparisons) */
+#ifndef LOLA_PAIRED
+#define LOLA_PAIRED 1
+#endif
+
 /* Per (tile, projection) setup kept in shared memory for the whole pass. */
 struct TileProj {
   float u0, v0, w0;   /* re-centred homogeneous coordinates at the tile origin */
   float cu, cv;       /* pixel offsets: ix = cu + u'/w, iy = cv + v'/w */
   float su[3], sv[3], sw[3]; /* per-axis steps (x, y, z) of u', v', w */
   int mode;
+  int pos;            /* MODE_FAST with non-negative detector coordinates only */
   int slot;
   float fx0, fx1, fy0, fy1;  /* footprint of the tile on the detector (pixels) */
   /* shared-memory staging (staged pass only) */
   int seq;                   /* index among the staged projections of the pass */
   int bx, by;                /* box origin in the padded image */
   float sbias;               /* 2^23 + box-local index of detector pixel (0, 0) */
+  float sxm, syo;            /* 2^23 + box-local column of detector column 0; box-local
+                                row of detector row 0 */
 };
 
 __device__ __forceinline__ float rcpApprox(float x)
@@ -318,11 +327,18 @@ struct PassArgs {
   unsigned long long tex[LOLA_MAX_BATCH];  /* texture layouts: object per ring slot */
 };
 
-/* Applies one projection to the thread's VPT voxels. */
+/* Voxel k of a thread's column in accumulators held as pairs (k, k+1) =
+ * (.x, .y); k is a compile-time constant after unrolling. */
+__device__ __forceinline__ float &voxel(float2 *v, int k)
+{
+  return (k & 1) ? v[k >> 1].y : v[k >> 1].x;
+}
+
+/* Applies one projection to the thread's VPT voxels, one voxel at a time. */
 template <int S, int VPT, bool KAHAN, bool CLAMP>
 __device__ __forceinline__ void applyProjection(const TileProj &tp, const void *img,
-    unsigned long long tex, const PassArgs &a, float fi, float fj, float (&acc)[VPT],
-    float (&comp)[VPT])
+    unsigned long long tex, const PassArgs &a, float fi, float fj, float2 (&acc)[VPT / 2],
+    float2 (&comp)[VPT / 2])
 {
   const float pitchF = (float)a.pitch;
   /* index = (ty + M) * pitch + (tx + M), formed as 2^23 + index in FP32 */
@@ -374,15 +390,128 @@ __device__ __forceinline__ void applyProjection(const TileProj &tp, const void *
     float term = val * (r * r);
     if (CLAMP)
       term = (val == 0.0f) ? 0.0f : term;  /* w = 0 would give 0 * inf */
+    float &ak = voxel(acc, k);
     if (KAHAN) {
-      const float y = term - comp[k];
-      const float s = acc[k] + y;
-      comp[k] = (s - acc[k]) - y;
-      acc[k] = s;
+      float &ck = voxel(comp, k);
+      const float y = term - ck;
+      const float s = ak + y;
+      ck = (s - ak) - y;
+      ak = s;
     } else {
-      acc[k] += term;
+      ak += term;
     }
   }
+}
+
+/* Applies one projection to the thread's VPT voxels two at a time: voxels
+ * (k, k+1) go through every FP32 operation together as one packed f32x2
+ * instruction (sm_100 family), half the issue slots of the scalar code, with
+ * the same operations per voxel except two: w, u and v step by two voxels from
+ * the first pair, and the floor comes from a round-down add.  Only for tiles
+ * with tp.pos (footprint inside the zero margin, coordinates >= 0), where C
+ * truncation is floor: floor(ix) is read from ix + 2^23 rounded down (the FMA
+ * pipe) instead of a float-to-integer conversion (the slower XU pipe), and the
+ * stored index is formed from the same sums.
+ *
+ * The stored pixel index is (floor(iy) + yo) * rowPitch + floor(ix) + xo.
+ * xm = 2^23 + xo must be an integer with xo + floor(ix) >= 0 for every voxel,
+ * so that ix + xm lies in [2^23, 2^24), where floats are the integers and the
+ * round-down sum is exact (KROW = false folds yo * rowPitch into xo, which
+ * needs the same of the whole offset).  fetch(k, idxf, fx, fy, p00, p10, p01,
+ * p11) reads voxel k's taps given idxf = 2^23 + its pixel index and floor(ix),
+ * floor(iy). */
+template <int VPT, bool KAHAN, bool KROW, class Fetch>
+__device__ __forceinline__ void pairedUpdate(const TileProj &tp, float fi, float fj, float xm,
+    float yo, float rowPitch, Fetch fetch, float2 (&acc)[VPT / 2], float2 (&comp)[VPT / 2])
+{
+  const float magic = 8388608.0f;  /* 2^23 */
+  const float2 kx = make_float2(xm, xm), nkx = make_float2(-xm, -xm);
+  const float2 ky = make_float2(magic, magic), nky = make_float2(-magic, -magic);
+  const float2 pitch2 = make_float2(rowPitch, rowPitch);
+  const float2 neg1 = make_float2(-1.0f, -1.0f);
+  const float2 yo2 = make_float2(yo, yo);
+
+  const float ut = fmaf(fj, tp.su[1], fmaf(fi, tp.su[0], tp.u0));
+  const float vt = fmaf(fj, tp.sv[1], fmaf(fi, tp.sv[0], tp.v0));
+  const float wt = fmaf(fj, tp.sw[1], fmaf(fi, tp.sw[0], tp.w0));
+  /* w, u and v step by two voxels from the first pair: one packed add per
+     coordinate and pair (two scalar FMAs from the pair's own k measured 6 %
+     slower for the issue slots they take) */
+  float2 U = make_float2(ut, ut + tp.su[2]);
+  float2 V = make_float2(vt, vt + tp.sv[2]);
+  float2 W = make_float2(wt, wt + tp.sw[2]);
+  const float2 dU = make_float2(2.0f * tp.su[2], 2.0f * tp.su[2]);
+  const float2 dV = make_float2(2.0f * tp.sv[2], 2.0f * tp.sv[2]);
+  const float2 dW = make_float2(2.0f * tp.sw[2], 2.0f * tp.sw[2]);
+  const float2 CU = make_float2(tp.cu, tp.cu), CV = make_float2(tp.cv, tp.cv);
+#pragma unroll
+  for (int j = 0; j < VPT / 2; ++j) {
+    if (j > 0) {
+      U = __fadd2_rn(U, dU);
+      V = __fadd2_rn(V, dV);
+      W = __fadd2_rn(W, dW);
+    }
+    const float2 R = make_float2(rcpApprox(W.x), rcpApprox(W.y));
+    const float2 IX = __ffma2_rn(U, R, CU);
+    const float2 IY = __ffma2_rn(V, R, CV);
+    const float2 XM = __fadd2_rd(IX, kx);  /* xm + floor(ix), exact */
+    const float2 YM = __fadd2_rd(IY, ky);  /* 2^23 + floor(iy) */
+    const float2 FX = __fadd2_rn(XM, nkx);
+    const float2 FY = __fadd2_rn(YM, nky);
+    const float2 AX = __ffma2_rn(FX, neg1, IX);  /* ix - floor(ix), exact */
+    const float2 AY = __ffma2_rn(FY, neg1, IY);
+    /* 2^23 + pixel index */
+    const float2 IDX = __ffma2_rn(KROW ? __fadd2_rn(FY, yo2) : FY, pitch2, XM);
+    float p00[2], p10[2], p01[2], p11[2];
+#pragma unroll
+    for (int h = 0; h < 2; ++h)
+      fetch(2 * j + h, h ? IDX.y : IDX.x, h ? FX.y : FX.x, h ? FY.y : FY.x, p00[h], p10[h],
+          p01[h], p11[h]);
+    const float2 P00 = make_float2(p00[0], p00[1]), P10 = make_float2(p10[0], p10[1]);
+    const float2 P01 = make_float2(p01[0], p01[1]), P11 = make_float2(p11[0], p11[1]);
+    const float2 B = __ffma2_rn(AX, __ffma2_rn(P00, neg1, P10), P00);
+    const float2 T = __ffma2_rn(AX, __ffma2_rn(P01, neg1, P11), P01);
+    const float2 VAL = __ffma2_rn(AY, __ffma2_rn(B, neg1, T), B);
+    const float2 RR = __fmul2_rn(R, R);
+    if (KAHAN) {
+      const float2 term = __fmul2_rn(VAL, RR);
+      const float2 y = __ffma2_rn(comp[j], neg1, term);
+      const float2 s = __fadd2_rn(acc[j], y);
+      comp[j] = __ffma2_rn(y, neg1, __ffma2_rn(acc[j], neg1, s));
+      acc[j] = s;
+    } else {
+      acc[j] = __ffma2_rn(VAL, RR, acc[j]);
+    }
+  }
+}
+
+/* The paired update on the stored ring (loads, texture or both). */
+template <int S, int VPT, bool KAHAN>
+__device__ __forceinline__ void applyPairs(const TileProj &tp, const void *img,
+    unsigned long long tex, const PassArgs &a, float fi, float fj, float2 (&acc)[VPT / 2],
+    float2 (&comp)[VPT / 2])
+{
+  const uint32_t maxIdx = Layout<S>::kQuad ? (uint32_t)(a.pitch * a.rows - 1)
+                                           : (uint32_t)(a.pitch * a.rows - a.pitch - 2);
+  const int pitch = a.pitch;
+  const float margin = (float)a.margin;
+  /* index = (fy + M) * pitch + (fx + M) */
+  const float xm = 8388608.0f + (float)(a.margin * a.pitch + a.margin);
+  auto fetch = [&](int k, float idxf, float fx, float fy, float &p00, float &p10, float &p01,
+                   float &p11) {
+    if constexpr (Layout<S>::kTex) {
+      texTaps(tex, fx + (margin + 1.0f), fy + (margin + 1.0f), p00, p10, p01, p11);
+    } else {
+      if (Layout<S>::kMixed && ((LOLA_MIXED_TEX_MASK >> k) & 1u)) {
+        texQuad(tex, fx + (margin + 0.5f), fy + (margin + 0.5f), p00, p10, p01, p11);
+      } else {
+        uint32_t idx = __float_as_uint(idxf) - 0x4B000000u;
+        idx = min(idx, maxIdx);  /* memory-safety net; never active on valid input */
+        Layout<S>::fetch(img, idx, pitch, p00, p10, p01, p11);
+      }
+    }
+  };
+  pairedUpdate<VPT, KAHAN, false>(tp, fi, fj, xm, 0.0f, (float)a.pitch, fetch, acc, comp);
 }
 
 /* Per-(tile, projection) setup shared by the pass kernels: the FP64 tile
@@ -426,6 +555,7 @@ __device__ __forceinline__ void setupTileGeom(const LolaPassProj *proj, int coun
       tp.sv[ax] = fmaf(-tp.cv, pp.step[ax][2], pp.step[ax][1]);
     }
     tp.mode = MODE_SLOW;
+    tp.pos = 0;
     tp.slot = pp.slot;
     sp[tid] = tp;
   }
@@ -472,6 +602,8 @@ __device__ __forceinline__ void setupTileGeom(const LolaPassProj *proj, int coun
       else
         mode = MODE_SLOW;
       sp[p].mode = mode;
+      /* C truncation equals floor where every coordinate is >= 0 */
+      sp[p].pos = (mode == MODE_FAST) && mnx - slack >= 0.0f && mny - slack >= 0.0f;
       sp[p].fx0 = mnx - slack;
       sp[p].fx1 = mxx + slack;
       sp[p].fy0 = mny - slack;
@@ -498,14 +630,16 @@ __device__ __forceinline__ void setupTile(const LolaPassParams &P, const PassArg
 }
 
 /* Resident blocks per SM requested from the register allocator.  The pass is
- * bound by the latency of its gathers, so occupancy pays: 48 warps per SM
- * (40 registers for 8 voxels x 8 rows) measured 25 % faster on GB300 than the
- * compiler's own choice of 61 registers and 32 warps.  LOLA_MIN_BLOCKS
- * overrides it at build time (0 = the compiler's choice). */
+ * bound by the latency of its gathers, so occupancy pays, up to the point
+ * where registers spill: measured on GB300 at N=1024, the one-voxel path ran
+ * best at 48 warps per SM (40 registers; 25 % faster than the compiler's own
+ * 61 registers and 32 warps), the paired path at 40 warps (48 registers:
+ * +9 % for f16qx, +6 % for f32 over 48 warps; 36 and 44 warps are slower).
+ * LOLA_MIN_BLOCKS overrides it at build time (0 = the compiler's choice). */
 template <int VPT, int ROWS> struct MinBlocks {
-  /* 8 voxels per thread: 48 warps per SM (40 registers); 16 voxels: 20-24
-     warps, which keeps their accumulators out of local memory */
-  static constexpr int kValue = (VPT <= 8) ? 1536 / (32 * ROWS) : 640 / (32 * ROWS);
+  /* 8 voxels per thread: 40 warps per SM; 16 voxels: 20-24 warps, which
+     keeps their accumulators out of local memory */
+  static constexpr int kValue = (VPT <= 8) ? 1280 / (32 * ROWS) : 640 / (32 * ROWS);
 };
 #ifdef LOLA_MIN_BLOCKS
 #define LOLA_PASS_MIN_BLOCKS(VPT, ROWS) LOLA_MIN_BLOCKS
@@ -545,11 +679,11 @@ __global__ void __launch_bounds__(32 * ROWS, LOLA_PASS_MIN_BLOCKS(VPT, ROWS))
   /* the plan holds only the slab z in [zBegin, zEnd) */
   float *vcol = a.volume + ((size_t)(z0 - P.zBegin) * N + (size_t)(inXY ? y : 0)) * (size_t)N +
                 (inXY ? x : 0);
-  float acc[VPT], comp[VPT];
+  float2 acc[VPT / 2], comp[VPT / 2];
 #pragma unroll
   for (int k = 0; k < VPT; ++k) {
-    acc[k] = (inXY && z0 + k < P.zEnd) ? vcol[k * slice] : 0.0f;
-    comp[k] = 0.0f;
+    voxel(acc, k) = (inXY && z0 + k < P.zEnd) ? vcol[k * slice] : 0.0f;
+    voxel(comp, k) = 0.0f;
   }
   const float fi = (float)threadIdx.x, fj = (float)threadIdx.y;
   for (int p = 0; p < count; ++p) {
@@ -560,7 +694,9 @@ __global__ void __launch_bounds__(32 * ROWS, LOLA_PASS_MIN_BLOCKS(VPT, ROWS))
     const void *img = static_cast<const char *>(a.ring) + (size_t)tp.slot * a.slotBytes;
     const unsigned long long tex =
         (Layout<S>::kTex || Layout<S>::kMixed) ? a.tex[tp.slot] : 0ull;
-    if (mode == MODE_FAST)
+    if (mode == MODE_FAST && tp.pos && LOLA_PAIRED)
+      applyPairs<S, VPT, KAHAN>(tp, img, tex, a, fi, fj, acc, comp);
+    else if (mode == MODE_FAST)
       applyProjection<S, VPT, KAHAN, false>(tp, img, tex, a, fi, fj, acc, comp);
     else
       applyProjection<S, VPT, KAHAN, true>(tp, img, tex, a, fi, fj, acc, comp);
@@ -568,7 +704,7 @@ __global__ void __launch_bounds__(32 * ROWS, LOLA_PASS_MIN_BLOCKS(VPT, ROWS))
 #pragma unroll
   for (int k = 0; k < VPT; ++k) {
     if (inXY && z0 + k < P.zEnd)
-      vcol[k * slice] = KAHAN ? (acc[k] - comp[k]) : acc[k];
+      vcol[k * slice] = KAHAN ? (voxel(acc, k) - voxel(comp, k)) : voxel(acc, k);
   }
 }
 

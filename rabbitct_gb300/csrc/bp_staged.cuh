@@ -189,7 +189,7 @@ template <> struct SharedTaps<LOLA_STORE_F32QX> : SharedTaps<LOLA_STORE_F32Q> {}
  * tiles on the fast path are staged). */
 template <int S, int VPT, bool KAHAN>
 __device__ __forceinline__ void applyStaged(const TileProj &tp, const unsigned char *box,
-    const StageArgs &g, float fi, float fj, float (&acc)[VPT], float (&comp)[VPT])
+    const StageArgs &g, float fi, float fj, float2 (&acc)[VPT / 2], float2 (&comp)[VPT / 2])
 {
   const float bw = (float)g.boxW;
   const uint32_t maxIdx = SharedTaps<S>::kQuad ? (uint32_t)(g.boxW * g.boxH - 1)
@@ -219,15 +219,37 @@ __device__ __forceinline__ void applyStaged(const TileProj &tp, const unsigned c
     const float t = fmaf(ax, p11 - p01, p01);
     const float val = fmaf(ay, t - b, b);
     const float term = val * (r * r);
+    float &ak = voxel(acc, k);
     if (KAHAN) {
-      const float y = term - comp[k];
-      const float s = acc[k] + y;
-      comp[k] = (s - acc[k]) - y;
-      acc[k] = s;
+      float &ck = voxel(comp, k);
+      const float y = term - ck;
+      const float s = ak + y;
+      ck = (s - ak) - y;
+      ak = s;
     } else {
-      acc[k] += term;
+      ak += term;
     }
   }
+}
+
+/* The paired update (pairedUpdate) on a staged box: the same arithmetic as
+ * applyPairs on the ring, so both gather paths give identical results. */
+template <int S, int VPT, bool KAHAN>
+__device__ __forceinline__ void applyStagedPairs(const TileProj &tp, const unsigned char *box,
+    const StageArgs &g, float fi, float fj, float2 (&acc)[VPT / 2], float2 (&comp)[VPT / 2])
+{
+  const uint32_t maxIdx = SharedTaps<S>::kQuad ? (uint32_t)(g.boxW * g.boxH - 1)
+                                               : (uint32_t)(g.boxW * g.boxH - g.boxW - 2);
+  const int boxW = g.boxW;
+  auto fetch = [&](int, float idxf, float, float, float &p00, float &p10, float &p01,
+                   float &p11) {
+    uint32_t idx = __float_as_uint(idxf) - 0x4B000000u;
+    idx = min(idx, maxIdx);  /* stays inside the stage buffer whatever the input */
+    SharedTaps<S>::fetch(box, idx, boxW, p00, p10, p01, p11);
+  };
+  /* box-local column and row offsets kept apart: the box may start below
+     detector row 0's stored row, so only the column offset is non-negative */
+  pairedUpdate<VPT, KAHAN, true>(tp, fi, fj, tp.sxm, tp.syo, (float)g.boxW, fetch, acc, comp);
 }
 
 #ifndef LOLA_STAGED_MIN_BLOCKS
@@ -280,6 +302,8 @@ __global__ void __launch_bounds__(32 * (ROWS + 1), LOLA_STAGED_MIN_BLOCKS)
       t.bx = bx;
       t.by = ylo;
       t.sbias = 8388608.0f + (float)((a.margin - bx) + (a.margin - ylo) * g.boxW);
+      t.sxm = 8388608.0f + (float)(a.margin - bx);
+      t.syo = (float)(a.margin - ylo);
     }
   }
   __syncthreads();
@@ -326,11 +350,11 @@ __global__ void __launch_bounds__(32 * (ROWS + 1), LOLA_STAGED_MIN_BLOCKS)
   /* the plan holds only the slab z in [zBegin, zEnd) */
   float *vcol = a.volume + ((size_t)(z0 - P.zBegin) * N + (size_t)(inXY ? y : 0)) * (size_t)N +
                 (inXY ? x : 0);
-  float acc[VPT], comp[VPT];
+  float2 acc[VPT / 2], comp[VPT / 2];
 #pragma unroll
   for (int k = 0; k < VPT; ++k) {
-    acc[k] = (inXY && z0 + k < P.zEnd) ? vcol[k * slice] : 0.0f;
-    comp[k] = 0.0f;
+    voxel(acc, k) = (inXY && z0 + k < P.zEnd) ? vcol[k * slice] : 0.0f;
+    voxel(comp, k) = 0.0f;
   }
   const float fi = (float)threadIdx.x, fj = (float)threadIdx.y;
   bool abandoned = false;
@@ -345,7 +369,10 @@ __global__ void __launch_bounds__(32 * (ROWS + 1), LOLA_STAGED_MIN_BLOCKS)
         atomicExch(g.errorFlag, 2);
         abandoned = true;
       }
-      if (!abandoned)
+      if (!abandoned && tp.pos && LOLA_PAIRED)
+        applyStagedPairs<S, VPT, KAHAN>(tp, stageMem + s * g.stageBytes, g, fi, fj, acc,
+            comp);
+      else if (!abandoned)
         applyStaged<S, VPT, KAHAN>(tp, stageMem + s * g.stageBytes, g, fi, fj, acc, comp);
       __syncwarp();
       if (threadIdx.x == 0)
@@ -355,7 +382,9 @@ __global__ void __launch_bounds__(32 * (ROWS + 1), LOLA_STAGED_MIN_BLOCKS)
     const void *img = static_cast<const char *>(a.ring) + (size_t)tp.slot * a.slotBytes;
     const unsigned long long tex =
         (Layout<S>::kTex || Layout<S>::kMixed) ? a.tex[tp.slot] : 0ull;
-    if (mode == MODE_FAST)
+    if (mode == MODE_FAST && tp.pos && LOLA_PAIRED)
+      applyPairs<S, VPT, KAHAN>(tp, img, tex, a, fi, fj, acc, comp);
+    else if (mode == MODE_FAST)
       applyProjection<S, VPT, KAHAN, false>(tp, img, tex, a, fi, fj, acc, comp);
     else
       applyProjection<S, VPT, KAHAN, true>(tp, img, tex, a, fi, fj, acc, comp);
@@ -363,7 +392,7 @@ __global__ void __launch_bounds__(32 * (ROWS + 1), LOLA_STAGED_MIN_BLOCKS)
 #pragma unroll
   for (int k = 0; k < VPT; ++k) {
     if (inXY && z0 + k < P.zEnd)
-      vcol[k * slice] = KAHAN ? (acc[k] - comp[k]) : acc[k];
+      vcol[k * slice] = KAHAN ? (voxel(acc, k) - voxel(comp, k)) : voxel(acc, k);
   }
 }
 
