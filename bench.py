@@ -41,16 +41,44 @@ import numpy as np  # noqa: E402
 
 METRIC = "GUPS (1e9 voxel updates/s) N=512,1024: FP16-stored vs FP32 path, RMSE vs FP64"
 
-# Algorithmic instructions per computed voxel update of the pass kernel's
-# method (FP32/INT issue slots): 3 FMA for u,v,w; 1 reciprocal; 2 FMA for the
-# pixel coordinates; 1 mul for 1/w^2; 2 truncations; 2 fraction subtractions;
-# 2 for the stored index (FMA + add) and 1 address; 6 for the two-level
-# bilinear lerp; 1 FMA accumulate = 21, plus the gather loads (4 plain, 1 quad)
-# and the widening of 16-bit taps to FP32 (4 per update).  The texture layouts
-# replace the index, address and widening work by 2 coordinate adds and one
-# 4-texel gather.
-INSTR_PER_UPDATE = {"f32": 25, "f16": 29, "bf16": 29, "f32q": 22, "f16q": 26, "bf16q": 26,
-                    "tex32": 21, "tex16": 21, "f16qx": 24, "f32qx": 22}
+# Issue slots per computed voxel update of the pass kernel's two implemented
+# sequences (hand count of the source, FP32/INT/memory instructions):
+#  - one voxel at a time (slow tiles, and fast tiles that touch negative
+#    detector coordinates): 3 FMA for u,v,w; 1 reciprocal; 2 FMA for the pixel
+#    coordinates; 2 truncations; 2 fraction subtractions; 6 for the two-level
+#    bilinear lerp; 2 for 1/w^2 and the weighted accumulate = 18, plus the
+#    stored index's FMA on the load path;
+#  - two voxels per packed f32x2 instruction (paired tiles): per pair 3 steps,
+#    2 coordinates, 6 floor/fraction, 1 index, 6 lerp, 2 weight+accumulate =
+#    20 packed + 2 reciprocals, i.e. 11 per voxel;
+# plus, per voxel and either way, its fetch: 2 index integer ops, 1 address,
+# the gathers (4 plain or 1 quad) and 4 widenings of 16-bit taps on the load
+# path, or 2 coordinate adds and 1 texture gather.  Mixed layouts fetch
+# MIXED_TEX_FRACTION of their voxels through the texture unit
+# (LOLA_MIXED_TEX_MASK = 0xAAAA in lolacuda_internal.h).
+MIXED_TEX_FRACTION = 0.5
+_LOAD_FETCH = {"f32": 7, "f16": 11, "bf16": 11, "f32q": 4, "f16q": 8, "bf16q": 8}
+_TEX_FETCH = 3
+
+
+def _fetch_cost(storage):
+    """(issue slots of a voxel's fetch, fraction of voxels on the load path)."""
+    if storage in ("tex32", "tex16"):
+        return _TEX_FETCH, 0.0
+    if storage in ("f16qx", "f32qx"):
+        load = _LOAD_FETCH["f16q" if storage == "f16qx" else "f32q"]
+        t = MIXED_TEX_FRACTION
+        return t * _TEX_FETCH + (1 - t) * load, 1 - t
+    return _LOAD_FETCH[storage], 1.0
+
+
+def instr_per_update(storage, paired_fraction):
+    fetch, load_frac = _fetch_cost(storage)
+    one = 18 + load_frac + fetch
+    two = 11 + fetch
+    return paired_fraction * two + (1 - paired_fraction) * one
+
+
 STORAGE_IDS = {"f32": 0, "f16": 1, "bf16": 2, "f32q": 3, "f16q": 4, "bf16q": 5, "tex32": 6,
                "tex16": 7, "f16qx": 8, "f32qx": 9}
 
@@ -73,8 +101,8 @@ def parse_args():
     ap.add_argument("--storage", default="f16qx", choices=list(STORAGE_IDS))
     ap.add_argument("--fp32-storage", default="f32", choices=list(STORAGE_IDS))
     ap.add_argument("--batch", type=int, default=16)
-    ap.add_argument("--vpt", type=int, default=8)
-    ap.add_argument("--rows", type=int, default=8)
+    ap.add_argument("--vpt", type=int, default=16)
+    ap.add_argument("--rows", type=int, default=4)
     ap.add_argument("--autotune", type=int, default=1,
                     help="1: pick tile shape / batch / staging with lolaCudaAutotune on the "
                          "first 32 projections before timing (untimed)")
@@ -347,13 +375,17 @@ def roofline(args, lib, storage, st, probes, cfg=None) -> dict:
            "skipped_fraction": st.tilePassesSkipped / max(1, st.tilePassesSkipped +
                                                            st.tilePassesFast +
                                                            st.tilePassesSlow)}
+    computed_pairs = max(1, st.tilePassesFast + st.tilePassesSlow)
+    paired = st.tilePassesPaired / computed_pairs
+    out["paired_fraction"] = paired
     if probes:
-        issue = probes["issue_inst_per_s"] / INSTR_PER_UPDATE[storage] / 1e9
+        ipu = instr_per_update(storage, paired)
+        issue = probes["issue_inst_per_s"] / ipu / 1e9
         gather = probes["gather"][storage] / 1e9
         bound, peak = ("issue", issue) if issue <= gather else ("gather", gather)
         out.update({"bound": bound, "peak": peak, "frac": achieved / peak,
                     "peak_issue": issue, "peak_gather": gather,
-                    "instr_per_update": INSTR_PER_UPDATE[storage],
+                    "instr_per_update": round(ipu, 2),
                     "peak_source": "probe kernels on this GPU (lolaCudaProbeIssueRate / "
                                    "lolaCudaProbeGatherRate)"})
     # HBM view: volume read + write once per pass plus the stored projections

@@ -132,8 +132,8 @@ enum {
   LOLA_BATCH_PERSISTENT = 1 /* one persistent pass launch per wave over all jobs */
 };
 
-/* Defaults: FP32 storage, plain accumulation, batch 16, 8 voxels per thread,
- * 8 rows per block, syncEachCall 1, exitOnError 1, no stats, device 0,
+/* Defaults: FP32 storage, plain accumulation, batch 16, 16 voxels per thread,
+ * 4 rows per block, syncEachCall 1, exitOnError 1, no stats, device 0,
  * staging 0.
  * Environment overrides read by lolaCudaDefaultConfig: LOLACUDA_STORAGE
  * (f32|f16|bf16|f32q|f16q|bf16q|tex32|tex16|f16qx|f32qx), LOLACUDA_ACCUM (plain|kahan),
@@ -176,6 +176,7 @@ typedef struct {
   int64_t stagedPasses;      /* passes launched with staging */
   int64_t overlappedPasses;  /* passes run in z-chunks to overlap a volume transfer */
   int64_t chunkLaunches;     /* kernel launches of those passes */
+  int64_t tilePassesPaired;  /* fast-path pairs run two voxels per packed instruction */
 } LolaCudaStats;
 
 typedef struct LolaCudaPlan LolaCudaPlan;

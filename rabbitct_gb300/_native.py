@@ -108,7 +108,8 @@ class LolaCudaStats(C.Structure):
                 ("tilePassesStaged", C.c_int64),
                 ("stagedPasses", C.c_int64),
                 ("overlappedPasses", C.c_int64),
-                ("chunkLaunches", C.c_int64)]
+                ("chunkLaunches", C.c_int64),
+                ("tilePassesPaired", C.c_int64)]
 
 
 STORAGE = {"f32": 0, "f16": 1, "bf16": 2, "f32q": 3, "f16q": 4, "bf16q": 5, "tex32": 6,

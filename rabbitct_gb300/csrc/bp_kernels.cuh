@@ -322,7 +322,7 @@ struct PassArgs {
   const void *ring;
   size_t slotBytes;
   float *volume;
-  unsigned long long *tileCounters;  /* [skip, fast, slow] or null */
+  unsigned long long *tileCounters;  /* LOLA_TILE_COUNTERS entries or null */
   int width, height, margin, pitch, rows;
   unsigned long long tex[LOLA_MAX_BATCH];  /* texture layouts: object per ring slot */
 };
@@ -630,25 +630,29 @@ __device__ __forceinline__ void setupTile(const LolaPassParams &P, const PassArg
 }
 
 /* Resident blocks per SM requested from the register allocator.  The pass is
- * bound by the latency of its gathers, so occupancy pays, up to the point
- * where registers spill: measured on GB300 at N=1024, the one-voxel path ran
- * best at 48 warps per SM (40 registers; 25 % faster than the compiler's own
- * 61 registers and 32 warps), the paired path at 40 warps (48 registers:
- * +9 % for f16qx, +6 % for f32 over 48 warps; 36 and 44 warps are slower).
+ * bound by the latency of its gathers, so occupancy pays up to the point where
+ * registers spill.  Measured on GB300 at N=1024 (496 projections, 1248x960):
+ *  - 8 voxels per thread: 40 warps per SM (48 registers; the paired path at
+ *    48 warps spilled and ran 5-13 % slower, 36 warps 1-5 % slower);
+ *  - 16 voxels per thread: 28 warps for the layouts that widen 16-bit taps
+ *    (72 registers: f16qx 1337 GUPS vs 1286 at 32 warps and 1309 at 36) and
+ *    36 warps for FP32 ones (56 registers: f32 1151 GUPS vs 1115 at 32 and
+ *    1108 at 40).
  * LOLA_MIN_BLOCKS overrides it at build time (0 = the compiler's choice). */
-template <int VPT, int ROWS> struct MinBlocks {
-  /* 8 voxels per thread: 40 warps per SM; 16 voxels: 20-24 warps, which
-     keeps their accumulators out of local memory */
-  static constexpr int kValue = (VPT <= 8) ? 1280 / (32 * ROWS) : 640 / (32 * ROWS);
+template <int S, int VPT, int ROWS> struct MinBlocks {
+  static constexpr bool kWide32 = S == LOLA_STORE_F32 || S == LOLA_STORE_F32Q ||
+                                  S == LOLA_STORE_TEX32 || S == LOLA_STORE_F32QX;
+  static constexpr int kWarps = (VPT <= 8) ? 40 : (kWide32 ? 36 : 28);
+  static constexpr int kValue = kWarps / ROWS;
 };
 #ifdef LOLA_MIN_BLOCKS
-#define LOLA_PASS_MIN_BLOCKS(VPT, ROWS) LOLA_MIN_BLOCKS
+#define LOLA_PASS_MIN_BLOCKS(S, VPT, ROWS) LOLA_MIN_BLOCKS
 #else
-#define LOLA_PASS_MIN_BLOCKS(VPT, ROWS) (MinBlocks<VPT, ROWS>::kValue)
+#define LOLA_PASS_MIN_BLOCKS(S, VPT, ROWS) (MinBlocks<S, VPT, ROWS>::kValue)
 #endif
 
 template <int S, int VPT, int ROWS, bool KAHAN>
-__global__ void __launch_bounds__(32 * ROWS, LOLA_PASS_MIN_BLOCKS(VPT, ROWS))
+__global__ void __launch_bounds__(32 * ROWS, LOLA_PASS_MIN_BLOCKS(S, VPT, ROWS))
     passKernel(const PassArgs a, const LolaPassParams P)
 {
   __shared__ TileProj sp[LOLA_MAX_BATCH];
@@ -660,30 +664,38 @@ __global__ void __launch_bounds__(32 * ROWS, LOLA_PASS_MIN_BLOCKS(VPT, ROWS))
   setupTile<ROWS, VPT>(P, a, sp, tid, 32 * ROWS, x0, y0, z0);
 
   if (a.tileCounters != nullptr && tid == 0) {
-    unsigned long long nSkip = 0, nFast = 0, nSlow = 0;
+    unsigned long long nSkip = 0, nFast = 0, nSlow = 0, nPaired = 0;
     for (int p = 0; p < count; ++p) {
       const int m = sp[p].mode;
       nSkip += (m == MODE_SKIP);
       nFast += (m == MODE_FAST);
       nSlow += (m == MODE_SLOW);
+      nPaired += (m == MODE_FAST && sp[p].pos && LOLA_PAIRED);
     }
     atomicAdd(a.tileCounters + 0, nSkip);
     atomicAdd(a.tileCounters + 1, nFast);
     atomicAdd(a.tileCounters + 2, nSlow);
+    atomicAdd(a.tileCounters + 4, nPaired);
   }
 
   /* -- main: voxels in registers across the pass -- */
   const int x = x0 + threadIdx.x, y = y0 + threadIdx.y;
   const bool inXY = (x < N) && (y < N);
   const size_t slice = (size_t)N * (size_t)N;
-  /* the plan holds only the slab z in [zBegin, zEnd) */
-  float *vcol = a.volume + ((size_t)(z0 - P.zBegin) * N + (size_t)(inXY ? y : 0)) * (size_t)N +
-                (inXY ? x : 0);
+  /* the plan holds only the slab z in [zBegin, zEnd); the column address is
+     formed again for the store rather than kept live across the pass */
+  auto column = [&]() {
+    return a.volume + ((size_t)(z0 - P.zBegin) * N + (size_t)(inXY ? y : 0)) * (size_t)N +
+           (inXY ? x : 0);
+  };
   float2 acc[VPT / 2], comp[VPT / 2];
+  {
+    const float *vcol = column();
 #pragma unroll
-  for (int k = 0; k < VPT; ++k) {
-    voxel(acc, k) = (inXY && z0 + k < P.zEnd) ? vcol[k * slice] : 0.0f;
-    voxel(comp, k) = 0.0f;
+    for (int k = 0; k < VPT; ++k) {
+      voxel(acc, k) = (inXY && z0 + k < P.zEnd) ? vcol[k * slice] : 0.0f;
+      voxel(comp, k) = 0.0f;
+    }
   }
   const float fi = (float)threadIdx.x, fj = (float)threadIdx.y;
   for (int p = 0; p < count; ++p) {
@@ -701,6 +713,7 @@ __global__ void __launch_bounds__(32 * ROWS, LOLA_PASS_MIN_BLOCKS(VPT, ROWS))
     else
       applyProjection<S, VPT, KAHAN, true>(tp, img, tex, a, fi, fj, acc, comp);
   }
+  float *vcol = column();
 #pragma unroll
   for (int k = 0; k < VPT; ++k) {
     if (inXY && z0 + k < P.zEnd)

@@ -309,18 +309,20 @@ __global__ void __launch_bounds__(32 * (ROWS + 1), LOLA_STAGED_MIN_BLOCKS)
   __syncthreads();
 
   if (a.tileCounters != nullptr && tid == 0) {
-    unsigned long long n[4] = { 0, 0, 0, 0 };
+    unsigned long long n[5] = { 0, 0, 0, 0, 0 };
     for (int p = 0; p < count; ++p) {
       const int m = sp[p].mode;
       n[0] += (m == MODE_SKIP);
       n[1] += (m == MODE_FAST);
       n[2] += (m == MODE_SLOW);
       n[3] += (m == MODE_STAGED);
+      n[4] += ((m == MODE_FAST || m == MODE_STAGED) && sp[p].pos && LOLA_PAIRED);
     }
     atomicAdd(a.tileCounters + 0, n[0]);
     atomicAdd(a.tileCounters + 1, n[1] + n[3]);
     atomicAdd(a.tileCounters + 2, n[2]);
     atomicAdd(a.tileCounters + 3, n[3]);
+    atomicAdd(a.tileCounters + 4, n[4]);
   }
 
   if (threadIdx.y == ROWS) {

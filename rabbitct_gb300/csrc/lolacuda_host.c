@@ -102,8 +102,10 @@ void lolaCudaDefaultConfig(LolaCudaConfig *c)
   c->storage = LOLA_STORE_F32;
   c->accumulation = LOLA_ACCUM_PLAIN;
   c->batch = 16;
-  c->voxelsPerThread = 8;
-  c->rowsPerBlock = 8;
+  /* 16 x 4 tiles: the fastest shape measured for FP32 and FP16 storage at
+     N=1024 on GB300 (f32 1151, f16qx 1337 GUPS vs 1026 and 1224 for 8 x 8) */
+  c->voxelsPerThread = 16;
+  c->rowsPerBlock = 4;
   c->syncEachCall = 1;
   c->exitOnError = 1;
   c->collectStats = 0;
@@ -363,8 +365,9 @@ static int planInit(LolaCudaPlan *p)
     }
   }
   CUDA_TRY(cudaMalloc((void **)&p->d_stage, (size_t)p->cfg.batch * p->imageElems * sizeof(float)));
-  CUDA_TRY(cudaMalloc((void **)&p->d_counters, 4 * sizeof(unsigned long long)));
-  CUDA_TRY(cudaMemsetAsync(p->d_counters, 0, 4 * sizeof(unsigned long long), p->stream));
+  CUDA_TRY(cudaMalloc((void **)&p->d_counters, LOLA_TILE_COUNTERS * sizeof(unsigned long long)));
+  CUDA_TRY(cudaMemsetAsync(p->d_counters, 0, LOLA_TILE_COUNTERS * sizeof(unsigned long long),
+      p->stream));
   CUDA_TRY(cudaMalloc((void **)&p->d_error, sizeof(int)));
   CUDA_TRY(cudaMemsetAsync(p->d_error, 0, sizeof(int), p->stream));
   CUDA_TRY(cudaEventRecord(p->stageFree, p->stream));
@@ -992,12 +995,13 @@ int lolaCudaPlanGetStats(LolaCudaPlan *p, LolaCudaStats *out)
     return 0;
   if (!collectEvents(p))
     return 0;
-  unsigned long long c[4] = { 0, 0, 0, 0 };
+  unsigned long long c[LOLA_TILE_COUNTERS] = { 0, 0, 0, 0, 0 };
   CUDA_TRY(cudaMemcpy(c, p->d_counters, sizeof(c), cudaMemcpyDeviceToHost));
   p->stats.tilePassesSkipped = (int64_t)c[0];
   p->stats.tilePassesFast = (int64_t)c[1];
   p->stats.tilePassesSlow = (int64_t)c[2];
   p->stats.tilePassesStaged = (int64_t)c[3];
+  p->stats.tilePassesPaired = (int64_t)c[4];
   *out = p->stats;
   return 1;
 }
@@ -1009,7 +1013,7 @@ int lolaCudaPlanResetStats(LolaCudaPlan *p)
   if (!lolaCudaPlanSynchronize(p) || !collectEvents(p))
     return 0;
   memset(&p->stats, 0, sizeof(p->stats));
-  CUDA_TRY(cudaMemset(p->d_counters, 0, 4 * sizeof(unsigned long long)));
+  CUDA_TRY(cudaMemset(p->d_counters, 0, LOLA_TILE_COUNTERS * sizeof(unsigned long long)));
   return 1;
 }
 

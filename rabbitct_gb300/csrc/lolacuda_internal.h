@@ -1,5 +1,7 @@
-/* Internal interface between the C host code (lolacuda_host.c) and the CUDA
- * kernels (lolacuda_kernels.cu).  Plain C types only. */
+/* Internal interface between the C host code (lolacuda_host.c,
+ * lolacuda_file.c, lolacuda_result.c) and the CUDA side (bp_*.cu kernels,
+ * lolacuda_dispatch.cu launchers, lolacuda_batch.cu, lolacuda_verify.cu).
+ * Plain C types only. */
 #ifndef LOLACUDA_INTERNAL_H
 #define LOLACUDA_INTERNAL_H
 
@@ -57,22 +59,28 @@ typedef struct {
   LolaPassProj proj[LOLA_MAX_BATCH];
 } LolaPassParams;
 
+/* Per-plan tile counters of the pass kernels: (tile, projection) pairs
+ * skipped, fast (staged included), slow, staged, and fast on the paired path. */
+#define LOLA_TILE_COUNTERS 5
+
 /* Mixed layouts: voxels (bit k of each 8, per thread) that fetch through the
- * texture unit; 2 of every 8 measured best on GB300. */
+ * texture unit.  With the paired path (one load and one texture voxel per
+ * pair) 4 of every 8 measured best on GB300: +2.5 % over 2 of 8, 4 % over 1
+ * of 8 or none, 2 % over whole pairs through the texture unit. */
 #ifndef LOLA_MIXED_TEX_MASK
-#define LOLA_MIXED_TEX_MASK 0x8888u
+#define LOLA_MIXED_TEX_MASK 0xAAAAu
 #endif
 
 /* Stage buffers of the staged pass (a build-time tuning knob). */
 #ifndef LOLA_STAGES
 #define LOLA_STAGES 3
+#endif
 
 /* z-chunks of a volume transfer overlapped with a pass (upload before the
    first pass, download after the last one) */
 #define LOLA_XFER_CHUNKS 8
 /* volumes smaller than this move in one piece */
 #define LOLA_XFER_MIN_CHUNK_BYTES (32u << 20)
-#endif
 
 /* Shared-memory staging of one pass (bp_staged.cuh): the tensor map over the
  * stored ring and the staging box. */

@@ -121,18 +121,21 @@ def test_accumulates_into_initial_volume(lib, scan12):
     assert metrics.errors(vol, ref)["rel_rmse"] <= 1e-5
 
 
-def test_truncation_border_semantics(lib):
+@pytest.mark.parametrize("vpt,rows", [(8, 8), (16, 4)])
+def test_truncation_border_semantics(lib, vpt, rows):
     """A detector much smaller than the volume's shadow: many voxels project
     to u or v in (-2, 0), where LolaBunny's truncation gives negative weights,
-    and most tiles take the clamped or skipped paths."""
+    and many tiles reach past the 64-pixel zero margin (clamped path) or miss
+    the detector (skipped)."""
     from rabbitct_gb300.lolacuda import Plan
     spec = small_spec(width=64, height=48, nproj=9, seed=21)
-    spec.pitch = 0.308 * 1248 / 64 * 0.5   # half the field of view
+    spec.pitch = 0.308 * 1248 / 64 * 0.25   # a quarter of the field of view
     scan = synth.make_scan(spec)
     n = 48
     vs, o = _geom(n)
     ref = oracle.bunny_f64(n, vs, o, scan.matrices, scan.images)
-    with Plan(n, vs, o, spec.width, spec.height, batch=9, collect_stats=1) as plan:
+    with Plan(n, vs, o, spec.width, spec.height, batch=9, collect_stats=1,
+              voxels_per_thread=vpt, rows_per_block=rows) as plan:
         plan.backproject_host(scan.images, scan.matrices)
         vol = plan.download()
         st = plan.stats()
@@ -191,7 +194,8 @@ def test_staged_pass_matches_oracle_and_load_path(lib, storage, accum):
     vols = {}
     for staging in (1, 0):
         with Plan(n, vs, o, scan.width, scan.height, storage=storage, accumulation=accum,
-                  batch=5, staging=staging, collect_stats=1) as plan:
+                  batch=5, staging=staging, collect_stats=1, voxels_per_thread=8,
+                  rows_per_block=8) as plan:
             plan.backproject_host(scan.images, scan.matrices)
             vols[staging] = plan.download()
             st = plan.stats()
@@ -216,7 +220,7 @@ def test_staged_pass_ragged_volume_and_rows(lib):
     o = synth.origin_index(n, vs)
     ref = oracle.bunny_f64(n, vs, o, scan.matrices, scan.images)
     with Plan(n, vs, o, scan.width, scan.height, storage="f32", batch=10, rows_per_block=4,
-              collect_stats=1, staging=1) as plan:
+              voxels_per_thread=8, collect_stats=1, staging=1) as plan:
         plan.backproject_host(scan.images, scan.matrices)
         vol = plan.download()
         st = plan.stats()
@@ -258,6 +262,7 @@ def test_device_verification_matches_runner_metrics(lib, convert):
 def test_slabs_reassemble_unsharded_volume(lib):
     """Three tile-aligned z-slabs (as three GPUs would hold them) equal the
     unsharded volume bit for bit; an unaligned split agrees to rounding."""
+    from rabbitct_gb300._native import config
     from rabbitct_gb300.lolacuda import Plan, slab
     scan = synth.make_scan(small_spec(nproj=8, seed=44))
     n = 64
@@ -265,7 +270,8 @@ def test_slabs_reassemble_unsharded_volume(lib):
     with Plan(n, vs, o, scan.width, scan.height, batch=8) as plan:
         plan.backproject_host(scan.images, scan.matrices)
         whole = plan.download()
-    for align, exact in ((8, True), (1, False)):
+    tile = config().voxelsPerThread  # slabs on tile boundaries: identical tiles
+    for align, exact in ((tile, True), (1, False)):
         parts = []
         for r in range(3):
             b, c = slab(n, r, 3, align)
