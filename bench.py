@@ -404,8 +404,26 @@ def roofline(args, lib, storage, st, probes, cfg=None) -> dict:
                   "frac": hbm_gbs / hbm_peak,
                   "peak_source": "MEASURED_PEAKS.json" if "hbm_gbs" in peaks else "fallback",
                   "algorithmic_bytes_per_launch": vol_bytes + proj_bytes}
-    out["traffic"] = None
+    out["traffic"], out["traffic_source"] = dram_traffic(storage, vpt, rows, batch, args.n)
     return out
+
+
+TRAFFIC_FILE = ROOT / "profiles" / "passKernel_dram_n1024.txt"
+
+
+def dram_traffic(storage, vpt, rows, batch, n):
+    """dram__bytes_read.sum + dram__bytes_write.sum of one pass launch, from
+    the committed ncu capture of the same configuration (lines
+    `storage vpt rows batch n bytes`), or None when none matches."""
+    if not TRAFFIC_FILE.exists():
+        return None, None
+    for line in TRAFFIC_FILE.read_text().splitlines():
+        f = line.split()
+        if len(f) != 6 or line.startswith("#"):
+            continue
+        if (f[0], int(f[1]), int(f[2]), int(f[3]), int(f[4])) == (storage, vpt, rows, batch, n):
+            return float(f[5]), f"ncu capture, {TRAFFIC_FILE.relative_to(ROOT)}"
+    return None, None
 
 
 def time_e2e_slab(args, dist, scan, vs, o, storage) -> dict:
