@@ -16,6 +16,12 @@
 
 namespace lola {
 
+/* The stored-image geometry the per-projection updates read (the fields of
+ * PassArgs they use), held in registers for the current job. */
+struct ImageGeom {
+  int width, height, margin, pitch, rows;
+};
+
 template <int S>
 __global__ void __launch_bounds__(256) batchPackKernel(const LolaBatchWave w)
 {
@@ -46,6 +52,19 @@ __global__ void __launch_bounds__(256) batchPackKernel(const LolaBatchWave w)
 /* Resident blocks per SM for the batched pass; its per-job geometry lives in
  * registers rather than the constant bank, so it needs more of them than
  * passKernel (a build-time tuning knob). */
+/* 1: the batched pass takes the paired path on positive fast tiles like
+   passKernel (a build-time switch for comparisons) */
+#ifndef LOLA_BATCH_PAIRED
+#define LOLA_BATCH_PAIRED 1
+#endif
+
+/* Mixed layouts in the batched pass fetch every quad through loads: with
+   texture fetches in flight its per-item state no longer fits 64 registers
+   (1.4 KB of spills at the passKernel mask).  Same values either way. */
+#ifndef LOLA_BATCH_TEX_MASK
+#define LOLA_BATCH_TEX_MASK 0u
+#endif
+
 #ifndef LOLA_BATCH_MIN_BLOCKS
 #define LOLA_BATCH_MIN_BLOCKS 4
 #endif
@@ -123,7 +142,7 @@ __global__ void __launch_bounds__(256, LOLA_BATCH_MIN_BLOCKS) batchPassKernel(co
         if (mode == MODE_SKIP)
           continue;
         const TileProj tp = sp[p];
-        PassArgs a;
+        ImageGeom a;
         a.width = Jv->width;
         a.height = Jv->height;
         a.margin = Jv->margin;
@@ -132,12 +151,15 @@ __global__ void __launch_bounds__(256, LOLA_BATCH_MIN_BLOCKS) batchPassKernel(co
         const void *img = Jv->ring + (size_t)tp.slot * Jv->slotBytes;
         const unsigned long long tex =
             (Layout<S>::kTex || Layout<S>::kMixed) ? Jv->tex[tp.slot] : 0ull;
-        if (mode == MODE_FAST && tp.pos && LOLA_PAIRED)
-          applyPairs<S, VPT, KAHAN>(tp, img, tex, a, fi, fj, acc, comp);
+        if (mode == MODE_FAST && tp.pos && LOLA_PAIRED && LOLA_BATCH_PAIRED)
+          applyPairs<S, VPT, KAHAN, ImageGeom, LOLA_BATCH_TEX_MASK>(tp, img, tex, a, fi, fj,
+              acc, comp);
         else if (mode == MODE_FAST)
-          applyProjection<S, VPT, KAHAN, false>(tp, img, tex, a, fi, fj, acc, comp);
+          applyProjection<S, VPT, KAHAN, false, ImageGeom, LOLA_BATCH_TEX_MASK>(tp, img, tex, a,
+              fi, fj, acc, comp);
         else
-          applyProjection<S, VPT, KAHAN, true>(tp, img, tex, a, fi, fj, acc, comp);
+          applyProjection<S, VPT, KAHAN, true, ImageGeom, LOLA_BATCH_TEX_MASK>(tp, img, tex, a,
+              fi, fj, acc, comp);
       }
       float *vcol = J.volume + ((size_t)z0 * N + (size_t)(inXY ? y : 0)) * (size_t)N +
                     (inXY ? x : 0);

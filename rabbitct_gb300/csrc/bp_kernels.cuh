@@ -335,9 +335,14 @@ __device__ __forceinline__ float &voxel(float2 *v, int k)
 }
 
 /* Applies one projection to the thread's VPT voxels, one voxel at a time. */
-template <int S, int VPT, bool KAHAN, bool CLAMP>
+/* A (PassArgs, or the batched pass's ImageGeom) supplies width, height,
+ * margin, pitch and rows of the stored image.  TEXMASK: the voxels a mixed
+ * layout fetches through the texture unit (the values are the same either
+ * way: the FP16 point fetch widens exactly). */
+template <int S, int VPT, bool KAHAN, bool CLAMP, class A,
+    unsigned TEXMASK = LOLA_MIXED_TEX_MASK>
 __device__ __forceinline__ void applyProjection(const TileProj &tp, const void *img,
-    unsigned long long tex, const PassArgs &a, float fi, float fj, float2 (&acc)[VPT / 2],
+    unsigned long long tex, const A &a, float fi, float fj, float2 (&acc)[VPT / 2],
     float2 (&comp)[VPT / 2])
 {
   const float pitchF = (float)a.pitch;
@@ -375,7 +380,7 @@ __device__ __forceinline__ void applyProjection(const TileProj &tp, const void *
          texture; gathering at that + 1 selects it as the lower-left tap */
       const float off = (float)a.margin + 1.0f;
       texTaps(tex, tx + off, ty + off, p00, p10, p01, p11);
-    } else if (Layout<S>::kMixed && ((LOLA_MIXED_TEX_MASK >> k) & 1u)) {
+    } else if (Layout<S>::kMixed && ((TEXMASK >> k) & 1u)) {
       /* point fetch of texel (tx + M, ty + M): any coordinate inside it works */
       const float off = (float)a.margin + 0.5f;
       texQuad(tex, tx + off, ty + off, p00, p10, p01, p11);
@@ -413,23 +418,26 @@ __device__ __forceinline__ void applyProjection(const TileProj &tp, const void *
  * pipe) instead of a float-to-integer conversion (the slower XU pipe), and the
  * stored index is formed from the same sums.
  *
- * The stored pixel index is (floor(iy) + yo) * rowPitch + floor(ix) + xo.
- * xm = 2^23 + xo must be an integer with xo + floor(ix) >= 0 for every voxel,
- * so that ix + xm lies in [2^23, 2^24), where floats are the integers and the
- * round-down sum is exact (KROW = false folds yo * rowPitch into xo, which
- * needs the same of the whole offset).  fetch(k, idxf, fx, fy, p00, p10, p01,
- * p11) reads voxel k's taps given idxf = 2^23 + its pixel index and floor(ix),
- * floor(iy). */
-template <int VPT, bool KAHAN, bool KROW, class Fetch>
-__device__ __forceinline__ void pairedUpdate(const TileProj &tp, float fi, float fj, float xm,
-    float yo, float rowPitch, Fetch fetch, float2 (&acc)[VPT / 2], float2 (&comp)[VPT / 2])
+ * The tile's pixel offsets (cu, cv) are integers, so floor(ix) = cu + floor(q)
+ * with q = u'/w small (and of either sign): its fraction is exact and more
+ * precise than one taken of ix itself.  kxc = 2^23 + the stored index of pixel
+ * (cu, cv) in the image read (an integer); xm = kxc + floor(q) is the
+ * round-down sum q + kxc, exact because it lies in [2^23, 2^24) (it is 2^23 +
+ * the index of pixel (floor(ix), cv), and every such index of a paired tile is
+ * >= 0).  Likewise ym = 2^23 + cv + floor(qv) from qv + 2^23 + cv (floor(iy)
+ * >= 0), and the stored index of the voxel's pixel is
+ * xm + floor(qv) * rowPitch.
+ * fetch(k, idxf, fx, fy, p00, p10, p01, p11) reads voxel k's taps given
+ * idxf = 2^23 + its pixel index and floor(ix), floor(iy). */
+template <int VPT, bool KAHAN, class Fetch>
+__device__ __forceinline__ void pairedUpdate(const TileProj &tp, float fi, float fj, float kxc,
+    float rowPitch, Fetch fetch, float2 (&acc)[VPT / 2], float2 (&comp)[VPT / 2])
 {
   const float magic = 8388608.0f;  /* 2^23 */
-  const float2 kx = make_float2(xm, xm), nkx = make_float2(-xm, -xm);
-  const float2 ky = make_float2(magic, magic), nky = make_float2(-magic, -magic);
-  const float2 pitch2 = make_float2(rowPitch, rowPitch);
+  const float2 KX = make_float2(kxc, kxc);
+  const float2 KY = make_float2(magic + tp.cv, magic + tp.cv);
+  const float2 npitch = make_float2(-rowPitch, -rowPitch);
   const float2 neg1 = make_float2(-1.0f, -1.0f);
-  const float2 yo2 = make_float2(yo, yo);
 
   const float ut = fmaf(fj, tp.su[1], fmaf(fi, tp.su[0], tp.u0));
   const float vt = fmaf(fj, tp.sv[1], fmaf(fi, tp.sv[0], tp.v0));
@@ -443,7 +451,6 @@ __device__ __forceinline__ void pairedUpdate(const TileProj &tp, float fi, float
   const float2 dU = make_float2(2.0f * tp.su[2], 2.0f * tp.su[2]);
   const float2 dV = make_float2(2.0f * tp.sv[2], 2.0f * tp.sv[2]);
   const float2 dW = make_float2(2.0f * tp.sw[2], 2.0f * tp.sw[2]);
-  const float2 CU = make_float2(tp.cu, tp.cu), CV = make_float2(tp.cv, tp.cv);
 #pragma unroll
   for (int j = 0; j < VPT / 2; ++j) {
     if (j > 0) {
@@ -452,21 +459,20 @@ __device__ __forceinline__ void pairedUpdate(const TileProj &tp, float fi, float
       W = __fadd2_rn(W, dW);
     }
     const float2 R = make_float2(rcpApprox(W.x), rcpApprox(W.y));
-    const float2 IX = __ffma2_rn(U, R, CU);
-    const float2 IY = __ffma2_rn(V, R, CV);
-    const float2 XM = __fadd2_rd(IX, kx);  /* xm + floor(ix), exact */
-    const float2 YM = __fadd2_rd(IY, ky);  /* 2^23 + floor(iy) */
-    const float2 FX = __fadd2_rn(XM, nkx);
-    const float2 FY = __fadd2_rn(YM, nky);
-    const float2 AX = __ffma2_rn(FX, neg1, IX);  /* ix - floor(ix), exact */
-    const float2 AY = __ffma2_rn(FY, neg1, IY);
-    /* 2^23 + pixel index */
-    const float2 IDX = __ffma2_rn(KROW ? __fadd2_rn(FY, yo2) : FY, pitch2, XM);
+    const float2 Q = __fmul2_rn(U, R);    /* ix - cu */
+    const float2 QV = __fmul2_rn(V, R);   /* iy - cv */
+    const float2 XM = __fadd2_rd(Q, KX);  /* kxc + floor(q), exact */
+    const float2 YM = __fadd2_rd(QV, KY); /* 2^23 + cv + floor(qv), exact */
+    const float2 TX = __ffma2_rn(XM, neg1, KX);  /* -floor(q), exact */
+    const float2 TY = __ffma2_rn(YM, neg1, KY);  /* -floor(qv) */
+    const float2 AX = __fadd2_rn(Q, TX);  /* ix - floor(ix), exact */
+    const float2 AY = __fadd2_rn(QV, TY);
+    const float2 IDX = __ffma2_rn(TY, npitch, XM);  /* 2^23 + pixel index */
     float p00[2], p10[2], p01[2], p11[2];
 #pragma unroll
     for (int h = 0; h < 2; ++h)
-      fetch(2 * j + h, h ? IDX.y : IDX.x, h ? FX.y : FX.x, h ? FY.y : FY.x, p00[h], p10[h],
-          p01[h], p11[h]);
+      fetch(2 * j + h, h ? IDX.y : IDX.x, tp.cu - (h ? TX.y : TX.x),
+          tp.cv - (h ? TY.y : TY.x), p00[h], p10[h], p01[h], p11[h]);
     const float2 P00 = make_float2(p00[0], p00[1]), P10 = make_float2(p10[0], p10[1]);
     const float2 P01 = make_float2(p01[0], p01[1]), P11 = make_float2(p11[0], p11[1]);
     const float2 B = __ffma2_rn(AX, __ffma2_rn(P00, neg1, P10), P00);
@@ -486,23 +492,24 @@ __device__ __forceinline__ void pairedUpdate(const TileProj &tp, float fi, float
 }
 
 /* The paired update on the stored ring (loads, texture or both). */
-template <int S, int VPT, bool KAHAN>
+template <int S, int VPT, bool KAHAN, class A, unsigned TEXMASK = LOLA_MIXED_TEX_MASK>
 __device__ __forceinline__ void applyPairs(const TileProj &tp, const void *img,
-    unsigned long long tex, const PassArgs &a, float fi, float fj, float2 (&acc)[VPT / 2],
+    unsigned long long tex, const A &a, float fi, float fj, float2 (&acc)[VPT / 2],
     float2 (&comp)[VPT / 2])
 {
   const uint32_t maxIdx = Layout<S>::kQuad ? (uint32_t)(a.pitch * a.rows - 1)
                                            : (uint32_t)(a.pitch * a.rows - a.pitch - 2);
   const int pitch = a.pitch;
   const float margin = (float)a.margin;
-  /* index = (fy + M) * pitch + (fx + M) */
-  const float xm = 8388608.0f + (float)(a.margin * a.pitch + a.margin);
+  /* 2^23 + stored index of pixel (cu, cv): (cv + M) * pitch + (cu + M) */
+  const float kxc = fmaf(tp.cv, (float)a.pitch,
+      8388608.0f + (float)(a.margin * a.pitch + a.margin) + tp.cu);
   auto fetch = [&](int k, float idxf, float fx, float fy, float &p00, float &p10, float &p01,
                    float &p11) {
     if constexpr (Layout<S>::kTex) {
       texTaps(tex, fx + (margin + 1.0f), fy + (margin + 1.0f), p00, p10, p01, p11);
     } else {
-      if (Layout<S>::kMixed && ((LOLA_MIXED_TEX_MASK >> k) & 1u)) {
+      if (Layout<S>::kMixed && ((TEXMASK >> k) & 1u)) {
         texQuad(tex, fx + (margin + 0.5f), fy + (margin + 0.5f), p00, p10, p01, p11);
       } else {
         uint32_t idx = __float_as_uint(idxf) - 0x4B000000u;
@@ -511,7 +518,7 @@ __device__ __forceinline__ void applyPairs(const TileProj &tp, const void *img,
       }
     }
   };
-  pairedUpdate<VPT, KAHAN, false>(tp, fi, fj, xm, 0.0f, (float)a.pitch, fetch, acc, comp);
+  pairedUpdate<VPT, KAHAN>(tp, fi, fj, kxc, (float)a.pitch, fetch, acc, comp);
 }
 
 /* Per-(tile, projection) setup shared by the pass kernels: the FP64 tile
@@ -540,8 +547,9 @@ __device__ __forceinline__ void setupTileGeom(const LolaPassProj *proj, int coun
     const double U = m[0] * X + m[3] * Y + m[6] * Z + m[9];
     const double V = m[1] * X + m[4] * Y + m[7] * Z + m[10];
     const double Wd = m[2] * X + m[5] * Y + m[8] * Z + m[11];
-    const float cu = (float)U / (float)Wd;
-    const float cv = (float)V / (float)Wd;
+    /* integer pixel offsets: floor(ix) = cu + floor(u'/w) on the paired path */
+    const float cu = rintf((float)U / (float)Wd);
+    const float cv = rintf((float)V / (float)Wd);
     TileProj tp;
     tp.cu = isfinite(cu) ? cu : 0.0f;
     tp.cv = isfinite(cv) ? cv : 0.0f;

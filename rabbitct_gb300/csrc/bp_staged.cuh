@@ -247,9 +247,10 @@ __device__ __forceinline__ void applyStagedPairs(const TileProj &tp, const unsig
     idx = min(idx, maxIdx);  /* stays inside the stage buffer whatever the input */
     SharedTaps<S>::fetch(box, idx, boxW, p00, p10, p01, p11);
   };
-  /* box-local column and row offsets kept apart: the box may start below
-     detector row 0's stored row, so only the column offset is non-negative */
-  pairedUpdate<VPT, KAHAN, true>(tp, fi, fj, tp.sxm, tp.syo, (float)g.boxW, fetch, acc, comp);
+  /* 2^23 + box-local index of pixel (cu, cv), which lies in the box (the tile
+     origin's own pixel is inside its footprint) */
+  const float kxc = fmaf(tp.cv + tp.syo, (float)g.boxW, tp.sxm + tp.cu);
+  pairedUpdate<VPT, KAHAN>(tp, fi, fj, kxc, (float)g.boxW, fetch, acc, comp);
 }
 
 #ifndef LOLA_STAGED_MIN_BLOCKS
