@@ -427,8 +427,9 @@ __device__ __forceinline__ void applyProjection(const TileProj &tp, const void *
  * >= 0).  Likewise ym = 2^23 + cv + floor(qv) from qv + 2^23 + cv (floor(iy)
  * >= 0), and the stored index of the voxel's pixel is
  * xm + floor(qv) * rowPitch.
- * fetch(k, idxf, fx, fy, p00, p10, p01, p11) reads voxel k's taps given
- * idxf = 2^23 + its pixel index and floor(ix), floor(iy). */
+ * fetch(k, idxf, nqx, nqy, p00, p10, p01, p11) reads voxel k's taps given
+ * idxf = 2^23 + its pixel index, and nqx = cu - floor(ix), nqy = cv - floor(iy)
+ * (integers). */
 template <int VPT, bool KAHAN, class Fetch>
 __device__ __forceinline__ void pairedUpdate(const TileProj &tp, float fi, float fj, float kxc,
     float rowPitch, Fetch fetch, float2 (&acc)[VPT / 2], float2 (&comp)[VPT / 2])
@@ -471,8 +472,8 @@ __device__ __forceinline__ void pairedUpdate(const TileProj &tp, float fi, float
     float p00[2], p10[2], p01[2], p11[2];
 #pragma unroll
     for (int h = 0; h < 2; ++h)
-      fetch(2 * j + h, h ? IDX.y : IDX.x, tp.cu - (h ? TX.y : TX.x),
-          tp.cv - (h ? TY.y : TY.x), p00[h], p10[h], p01[h], p11[h]);
+      fetch(2 * j + h, h ? IDX.y : IDX.x, h ? TX.y : TX.x, h ? TY.y : TY.x, p00[h], p10[h],
+          p01[h], p11[h]);
     const float2 P00 = make_float2(p00[0], p00[1]), P10 = make_float2(p10[0], p10[1]);
     const float2 P01 = make_float2(p01[0], p01[1]), P11 = make_float2(p11[0], p11[1]);
     const float2 B = __ffma2_rn(AX, __ffma2_rn(P00, neg1, P10), P00);
@@ -504,13 +505,19 @@ __device__ __forceinline__ void applyPairs(const TileProj &tp, const void *img,
   /* 2^23 + stored index of pixel (cu, cv): (cv + M) * pitch + (cu + M) */
   const float kxc = fmaf(tp.cv, (float)a.pitch,
       8388608.0f + (float)(a.margin * a.pitch + a.margin) + tp.cu);
-  auto fetch = [&](int k, float idxf, float fx, float fy, float &p00, float &p10, float &p01,
+  /* texture coordinate of pixel (cu, cv): +1 selects it as the lower-left tap
+     of a tld4 gather, +0.5 is the centre of its texel for a point fetch; the
+     voxel's coordinate is that minus (cu - floor(ix)), exact (integers and
+     halves) */
+  const float toff = margin + (Layout<S>::kTex ? 1.0f : 0.5f);
+  const float tcx = tp.cu + toff, tcy = tp.cv + toff;
+  auto fetch = [&](int k, float idxf, float nqx, float nqy, float &p00, float &p10, float &p01,
                    float &p11) {
     if constexpr (Layout<S>::kTex) {
-      texTaps(tex, fx + (margin + 1.0f), fy + (margin + 1.0f), p00, p10, p01, p11);
+      texTaps(tex, tcx - nqx, tcy - nqy, p00, p10, p01, p11);
     } else {
       if (Layout<S>::kMixed && ((TEXMASK >> k) & 1u)) {
-        texQuad(tex, fx + (margin + 0.5f), fy + (margin + 0.5f), p00, p10, p01, p11);
+        texQuad(tex, tcx - nqx, tcy - nqy, p00, p10, p01, p11);
       } else {
         uint32_t idx = __float_as_uint(idxf) - 0x4B000000u;
         idx = min(idx, maxIdx);  /* memory-safety net; never active on valid input */
