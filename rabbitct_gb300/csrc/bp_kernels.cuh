@@ -78,6 +78,43 @@ __device__ __forceinline__ float rcpApprox(float x)
 __device__ __forceinline__ float bf16LoToFloat(uint32_t x) { return __uint_as_float(x << 16); }
 __device__ __forceinline__ float bf16HiToFloat(uint32_t x) { return __uint_as_float(x & 0xffff0000u); }
 
+/* ---- bilinear interpolation ------------------------------------------------- */
+
+/* 1: the 16-bit quad layouts store bilinear terms (below); 0: the four taps
+   (a build-time switch for comparisons) */
+#ifndef LOLA_QUAD_TERMS
+#define LOLA_QUAD_TERMS 1
+#endif
+
+/* The 16-bit quad layouts store each pixel's bilinear terms instead of its four
+ * taps: p00, p10 - p00, p01 - p00 and p11 - p01 - p10 + p00 (formed in FP32,
+ * then rounded), so that
+ *     bilinear = p00 + ax (p10 - p00) + ay ((p01 - p00) + ax (p11 - p01 - p10 + p00))
+ * takes three FMAs instead of six operations.  It is LolaBunny's product form
+ * (src/LolaBunny.c:24-29) regrouped; the 16-bit rounding falls on the terms
+ * instead of the taps. */
+__device__ __forceinline__ float4 bilinearTerms(float p00, float p10, float p01, float p11)
+{
+  const float d10 = p10 - p00;
+  return make_float4(p00, d10, p01 - p00, (p11 - p01) - d10);
+}
+
+/* Bilinear value from the four fetched terms: taps (p00, p10, p01, p11), or,
+ * for DIFF layouts, the terms of bilinearTerms. */
+template <bool DIFF>
+__device__ __forceinline__ float bilinear(float ax, float ay, float q0, float q1, float q2,
+    float q3)
+{
+  if (DIFF) {
+    const float b = fmaf(ax, q1, q0);
+    const float c = fmaf(ax, q3, q2);
+    return fmaf(ay, c, b);
+  }
+  const float b = fmaf(ax, q1 - q0, q0);
+  const float t = fmaf(ax, q3 - q2, q2);
+  return fmaf(ay, t - b, b);
+}
+
 /* ---- tap fetch per storage layout ------------------------------------------ */
 
 template <int S> struct Layout;
@@ -87,6 +124,7 @@ template <> struct Layout<LOLA_STORE_F32> {
   static constexpr bool kMixed = false;
   typedef float Elem;
   static constexpr bool kQuad = false;
+  static constexpr bool kDiff = false;
   __device__ static __forceinline__ void fetch(const void *img, uint32_t idx, int pitch,
       float &p00, float &p10, float &p01, float &p11)
   {
@@ -107,6 +145,7 @@ template <> struct Layout<LOLA_STORE_F16> {
   static constexpr bool kMixed = false;
   typedef __half Elem;
   static constexpr bool kQuad = false;
+  static constexpr bool kDiff = false;
   __device__ static __forceinline__ void fetch(const void *img, uint32_t idx, int pitch,
       float &p00, float &p10, float &p01, float &p11)
   {
@@ -127,6 +166,7 @@ template <> struct Layout<LOLA_STORE_BF16> {
   static constexpr bool kMixed = false;
   typedef __nv_bfloat16 Elem;
   static constexpr bool kQuad = false;
+  static constexpr bool kDiff = false;
   __device__ static __forceinline__ void fetch(const void *img, uint32_t idx, int pitch,
       float &p00, float &p10, float &p01, float &p11)
   {
@@ -147,6 +187,7 @@ template <> struct Layout<LOLA_STORE_F32Q> {
   static constexpr bool kMixed = false;
   typedef float4 Elem;
   static constexpr bool kQuad = true;
+  static constexpr bool kDiff = false;
   __device__ static __forceinline__ void fetch(const void *img, uint32_t idx, int,
       float &p00, float &p10, float &p01, float &p11)
   {
@@ -168,6 +209,7 @@ template <> struct Layout<LOLA_STORE_F16Q> {
   static constexpr bool kMixed = false;
   typedef uint2 Elem;
   static constexpr bool kQuad = true;
+  static constexpr bool kDiff = LOLA_QUAD_TERMS;
   __device__ static __forceinline__ void fetch(const void *img, uint32_t idx, int,
       float &p00, float &p10, float &p01, float &p11)
   {
@@ -185,8 +227,9 @@ template <> struct Layout<LOLA_STORE_F16Q> {
   __device__ static __forceinline__ void store(void *dst, size_t o, float a, float b, float c,
       float d)
   {
-    const __half2 lo = __floats2half2_rn(a, b);
-    const __half2 hi = __floats2half2_rn(c, d);
+    const float4 t = LOLA_QUAD_TERMS ? bilinearTerms(a, b, c, d) : make_float4(a, b, c, d);
+    const __half2 lo = __floats2half2_rn(t.x, t.y);
+    const __half2 hi = __floats2half2_rn(t.z, t.w);
     uint2 q;
     q.x = *reinterpret_cast<const uint32_t *>(&lo);
     q.y = *reinterpret_cast<const uint32_t *>(&hi);
@@ -199,6 +242,7 @@ template <> struct Layout<LOLA_STORE_BF16Q> {
   static constexpr bool kMixed = false;
   typedef uint2 Elem;
   static constexpr bool kQuad = true;
+  static constexpr bool kDiff = LOLA_QUAD_TERMS;
   __device__ static __forceinline__ void fetch(const void *img, uint32_t idx, int,
       float &p00, float &p10, float &p01, float &p11)
   {
@@ -211,8 +255,9 @@ template <> struct Layout<LOLA_STORE_BF16Q> {
   __device__ static __forceinline__ void store(void *dst, size_t o, float a, float b, float c,
       float d)
   {
-    const __nv_bfloat162 lo = __floats2bfloat162_rn(a, b);
-    const __nv_bfloat162 hi = __floats2bfloat162_rn(c, d);
+    const float4 t = LOLA_QUAD_TERMS ? bilinearTerms(a, b, c, d) : make_float4(a, b, c, d);
+    const __nv_bfloat162 lo = __floats2bfloat162_rn(t.x, t.y);
+    const __nv_bfloat162 hi = __floats2bfloat162_rn(t.z, t.w);
     uint2 q;
     q.x = *reinterpret_cast<const uint32_t *>(&lo);
     q.y = *reinterpret_cast<const uint32_t *>(&hi);
@@ -231,6 +276,7 @@ template <> struct Layout<LOLA_STORE_TEX32> {
   static constexpr bool kMixed = false;
   typedef float Elem;
   static constexpr bool kQuad = false;
+  static constexpr bool kDiff = false;
   __device__ static __forceinline__ void store(void *dst, size_t o, float a, float, float, float)
   {
     static_cast<float *>(dst)[o] = a;
@@ -242,6 +288,7 @@ template <> struct Layout<LOLA_STORE_TEX16> {
   static constexpr bool kMixed = false;
   typedef __half Elem;
   static constexpr bool kQuad = false;
+  static constexpr bool kDiff = false;
   __device__ static __forceinline__ void store(void *dst, size_t o, float a, float, float, float)
   {
     static_cast<__half *>(dst)[o] = __float2half_rn(a);
@@ -389,9 +436,7 @@ __device__ __forceinline__ void applyProjection(const TileProj &tp, const void *
       idx = min(idx, maxIdx);  /* memory-safety net; never active on valid input */
       Layout<S>::fetch(img, idx, a.pitch, p00, p10, p01, p11);
     }
-    const float b = fmaf(ax, p10 - p00, p00);
-    const float t = fmaf(ax, p11 - p01, p01);
-    const float val = fmaf(ay, t - b, b);
+    const float val = bilinear<Layout<S>::kDiff>(ax, ay, p00, p10, p01, p11);
     float term = val * (r * r);
     if (CLAMP)
       term = (val == 0.0f) ? 0.0f : term;  /* w = 0 would give 0 * inf */
@@ -430,7 +475,7 @@ __device__ __forceinline__ void applyProjection(const TileProj &tp, const void *
  * fetch(k, idxf, nqx, nqy, p00, p10, p01, p11) reads voxel k's taps given
  * idxf = 2^23 + its pixel index, and nqx = cu - floor(ix), nqy = cv - floor(iy)
  * (integers). */
-template <int VPT, bool KAHAN, class Fetch>
+template <int VPT, bool KAHAN, bool DIFF, class Fetch>
 __device__ __forceinline__ void pairedUpdate(const TileProj &tp, float fi, float fj, float kxc,
     float rowPitch, Fetch fetch, float2 (&acc)[VPT / 2], float2 (&comp)[VPT / 2])
 {
@@ -476,9 +521,16 @@ __device__ __forceinline__ void pairedUpdate(const TileProj &tp, float fi, float
           p01[h], p11[h]);
     const float2 P00 = make_float2(p00[0], p00[1]), P10 = make_float2(p10[0], p10[1]);
     const float2 P01 = make_float2(p01[0], p01[1]), P11 = make_float2(p11[0], p11[1]);
-    const float2 B = __ffma2_rn(AX, __ffma2_rn(P00, neg1, P10), P00);
-    const float2 T = __ffma2_rn(AX, __ffma2_rn(P01, neg1, P11), P01);
-    const float2 VAL = __ffma2_rn(AY, __ffma2_rn(B, neg1, T), B);
+    float2 VAL;
+    if (DIFF) {  /* terms: p00, p10 - p00, p01 - p00, p11 - p01 - p10 + p00 */
+      const float2 B = __ffma2_rn(AX, P10, P00);
+      const float2 C = __ffma2_rn(AX, P11, P01);
+      VAL = __ffma2_rn(AY, C, B);
+    } else {
+      const float2 B = __ffma2_rn(AX, __ffma2_rn(P00, neg1, P10), P00);
+      const float2 T = __ffma2_rn(AX, __ffma2_rn(P01, neg1, P11), P01);
+      VAL = __ffma2_rn(AY, __ffma2_rn(B, neg1, T), B);
+    }
     const float2 RR = __fmul2_rn(R, R);
     if (KAHAN) {
       const float2 term = __fmul2_rn(VAL, RR);
@@ -525,7 +577,7 @@ __device__ __forceinline__ void applyPairs(const TileProj &tp, const void *img,
       }
     }
   };
-  pairedUpdate<VPT, KAHAN>(tp, fi, fj, kxc, (float)a.pitch, fetch, acc, comp);
+  pairedUpdate<VPT, KAHAN, Layout<S>::kDiff>(tp, fi, fj, kxc, (float)a.pitch, fetch, acc, comp);
 }
 
 /* Per-(tile, projection) setup shared by the pass kernels: the FP64 tile

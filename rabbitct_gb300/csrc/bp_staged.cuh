@@ -104,6 +104,7 @@ template <int S> struct SharedTaps;
 
 template <> struct SharedTaps<LOLA_STORE_F32> {
   static constexpr bool kQuad = false;
+  static constexpr bool kDiff = false;
   __device__ static __forceinline__ void fetch(const unsigned char *b, uint32_t i, int w,
       float &p00, float &p10, float &p01, float &p11)
   {
@@ -117,6 +118,7 @@ template <> struct SharedTaps<LOLA_STORE_F32> {
 
 template <> struct SharedTaps<LOLA_STORE_F16> {
   static constexpr bool kQuad = false;
+  static constexpr bool kDiff = false;
   __device__ static __forceinline__ void fetch(const unsigned char *b, uint32_t i, int w,
       float &p00, float &p10, float &p01, float &p11)
   {
@@ -130,6 +132,7 @@ template <> struct SharedTaps<LOLA_STORE_F16> {
 
 template <> struct SharedTaps<LOLA_STORE_BF16> {
   static constexpr bool kQuad = false;
+  static constexpr bool kDiff = false;
   __device__ static __forceinline__ void fetch(const unsigned char *b, uint32_t i, int w,
       float &p00, float &p10, float &p01, float &p11)
   {
@@ -143,6 +146,7 @@ template <> struct SharedTaps<LOLA_STORE_BF16> {
 
 template <> struct SharedTaps<LOLA_STORE_F32Q> {
   static constexpr bool kQuad = true;
+  static constexpr bool kDiff = false;
   __device__ static __forceinline__ void fetch(const unsigned char *b, uint32_t i, int,
       float &p00, float &p10, float &p01, float &p11)
   {
@@ -156,6 +160,7 @@ template <> struct SharedTaps<LOLA_STORE_F32Q> {
 
 template <> struct SharedTaps<LOLA_STORE_F16Q> {
   static constexpr bool kQuad = true;
+  static constexpr bool kDiff = LOLA_QUAD_TERMS;  /* as stored by Layout<S> */
   __device__ static __forceinline__ void fetch(const unsigned char *b, uint32_t i, int,
       float &p00, float &p10, float &p01, float &p11)
   {
@@ -171,6 +176,7 @@ template <> struct SharedTaps<LOLA_STORE_F16Q> {
 
 template <> struct SharedTaps<LOLA_STORE_BF16Q> {
   static constexpr bool kQuad = true;
+  static constexpr bool kDiff = LOLA_QUAD_TERMS;  /* as stored by Layout<S> */
   __device__ static __forceinline__ void fetch(const unsigned char *b, uint32_t i, int,
       float &p00, float &p10, float &p01, float &p11)
   {
@@ -215,9 +221,7 @@ __device__ __forceinline__ void applyStaged(const TileProj &tp, const unsigned c
     idx = min(idx, maxIdx);  /* stays inside the stage buffer whatever the input */
     float p00, p10, p01, p11;
     SharedTaps<S>::fetch(box, idx, g.boxW, p00, p10, p01, p11);
-    const float b = fmaf(ax, p10 - p00, p00);
-    const float t = fmaf(ax, p11 - p01, p01);
-    const float val = fmaf(ay, t - b, b);
+    const float val = bilinear<SharedTaps<S>::kDiff>(ax, ay, p00, p10, p01, p11);
     const float term = val * (r * r);
     float &ak = voxel(acc, k);
     if (KAHAN) {
@@ -250,7 +254,8 @@ __device__ __forceinline__ void applyStagedPairs(const TileProj &tp, const unsig
   /* 2^23 + box-local index of pixel (cu, cv), which lies in the box (the tile
      origin's own pixel is inside its footprint) */
   const float kxc = fmaf(tp.cv + tp.syo, (float)g.boxW, tp.sxm + tp.cu);
-  pairedUpdate<VPT, KAHAN>(tp, fi, fj, kxc, (float)g.boxW, fetch, acc, comp);
+  pairedUpdate<VPT, KAHAN, SharedTaps<S>::kDiff>(tp, fi, fj, kxc, (float)g.boxW, fetch, acc,
+      comp);
 }
 
 #ifndef LOLA_STAGED_MIN_BLOCKS
