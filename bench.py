@@ -55,8 +55,11 @@ METRIC = "GUPS (1e9 voxel updates/s) N=512,1024: FP16-stored vs FP32 path, RMSE 
 # the gathers (4 plain or 1 quad) and 4 widenings of 16-bit taps on the load
 # path, or 2 coordinate adds and 1 texture gather.  Mixed layouts fetch
 # MIXED_TEX_FRACTION of their voxels through the texture unit
-# (LOLA_MIXED_TEX_MASK = 0xAAAA in lolacuda_internal.h).
+# (LOLA_MIXED_TEX_MASK = 0xAAAA in lolacuda_internal.h).  The 16-bit quad
+# layouts store bilinear terms, so their interpolation is 3 FMAs instead of 6
+# operations (3 issue slots less per voxel, 1.5 on the paired path).
 MIXED_TEX_FRACTION = 0.5
+_TERM_LAYOUTS = ("f16q", "bf16q", "f16qx")
 _LOAD_FETCH = {"f32": 7, "f16": 11, "bf16": 11, "f32q": 4, "f16q": 8, "bf16q": 8}
 _TEX_FETCH = 3
 
@@ -74,8 +77,9 @@ def _fetch_cost(storage):
 
 def instr_per_update(storage, paired_fraction):
     fetch, load_frac = _fetch_cost(storage)
-    one = 18 + load_frac + fetch
-    two = 11 + fetch
+    terms = storage in _TERM_LAYOUTS
+    one = (15 if terms else 18) + load_frac + fetch
+    two = (9.5 if terms else 11) + fetch
     return paired_fraction * two + (1 - paired_fraction) * one
 
 
