@@ -103,7 +103,11 @@ def parse_args():
     ap.add_argument("--width", type=int, default=1248)
     ap.add_argument("--height", type=int, default=960)
     ap.add_argument("--storage", default="f16qx", choices=list(STORAGE_IDS))
-    ap.add_argument("--fp32-storage", default="f32", choices=list(STORAGE_IDS))
+    ap.add_argument("--fp32-storage", default="f32", choices=list(STORAGE_IDS),
+                    help="the plain FP32 path (four FP32 taps per update)")
+    ap.add_argument("--fp32-quad-storage", default="f32q", choices=list(STORAGE_IDS) + ["none"],
+                    help="FP32 storage as 2x2 quads: the same exact FP32 taps and results as the "
+                         "plain path, one 16-byte load per update (none: skip)")
     ap.add_argument("--batch", type=int, default=16)
     ap.add_argument("--vpt", type=int, default=16)
     ap.add_argument("--rows", type=int, default=4)
@@ -112,7 +116,7 @@ def parse_args():
                          "first 32 projections before timing (untimed)")
     ap.add_argument("--staging", type=int, default=None,
                     help="1/0: force shared-memory staging on/off (default: library default)")
-    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--e2e-steps", type=int, default=4)
     ap.add_argument("--cpu-views", type=int, default=8,
                     help="projections in the bounded CPU-baseline sample")
     ap.add_argument("--shard", default="slabs", choices=["slabs", "replicas"],
@@ -547,13 +551,16 @@ def run_gpu(args, rank, world, local):
         probes = {"issue_inst_per_s": lib.lolaCudaProbeIssueRate(),
                   "gather": {s: lib.lolaCudaProbeGatherRate(STORAGE_IDS[s], scan.width,
                                                             scan.height)
-                             for s in {args.storage, args.fp32_storage}}}
+                             for s in {args.storage, args.fp32_storage,
+                                       args.fp32_quad_storage} - {"none"}}}
 
     clocks = ClockSampler(0)
     head = time_device(args, dist, lib, scan, vs, o, d_images, args.storage, clocks)
-    fp32 = None
+    fp32 = fp32q = None
     if not args.no_fp32 and args.fp32_storage != args.storage:
         fp32 = time_device(args, dist, lib, scan, vs, o, d_images, args.fp32_storage)
+    if not args.no_fp32 and args.fp32_quad_storage not in ("none", args.storage):
+        fp32q = time_device(args, dist, lib, scan, vs, o, d_images, args.fp32_quad_storage)
     d_images.free()
     if args.autotune:
         args.vpt = head["cfg"].voxelsPerThread
@@ -587,6 +594,14 @@ def run_gpu(args, rank, world, local):
                                                   probes, fp32["cfg"]),
                              "tuned": fp32["chosen"]}
         line["fp16_over_fp32"] = head["gups"] / fp32["gups"]
+    if fp32q is not None:
+        line["fp32_quads"] = {"value": fp32q["gups"], "unit": "GUPS",
+                              "storage": args.fp32_quad_storage,
+                              "ms_per_step": fp32q["ms"] / args.steps,
+                              "roofline": roofline(args, lib, args.fp32_quad_storage,
+                                                   fp32q["stats"], probes, fp32q["cfg"]),
+                              "tuned": fp32q["chosen"]}
+        line["fp16_over_fp32_quads"] = head["gups"] / fp32q["gups"]
     if e2e is not None:
         line["e2e"] = e2e
     if probes:

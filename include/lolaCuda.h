@@ -132,7 +132,8 @@ enum {
   LOLA_BATCH_PERSISTENT = 1 /* one persistent pass launch per wave over all jobs */
 };
 
-/* Defaults: FP32 storage, plain accumulation, batch 16, 16 voxels per thread,
+/* Defaults: FP32 quad storage (LOLA_STORE_F32Q: the same results as LOLA_STORE_F32,
+ * faster), plain accumulation, batch 16, 16 voxels per thread,
  * 4 rows per block, syncEachCall 1, exitOnError 1, no stats, device 0,
  * staging 0.
  * Environment overrides read by lolaCudaDefaultConfig: LOLACUDA_STORAGE

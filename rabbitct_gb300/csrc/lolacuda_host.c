@@ -99,7 +99,10 @@ static int envInt(const char *name, int dflt)
 void lolaCudaDefaultConfig(LolaCudaConfig *c)
 {
   memset(c, 0, sizeof(*c));
-  c->storage = LOLA_STORE_F32;
+  /* FP32 2x2 quads: the exact FP32 taps of plain FP32 storage and identical
+     results, one 16-byte load per update instead of four 4-byte loads
+     (1282 vs 1132 GUPS at N=1024 on GB300) */
+  c->storage = LOLA_STORE_F32Q;
   c->accumulation = LOLA_ACCUM_PLAIN;
   c->batch = 16;
   /* 16 x 4 tiles: the fastest shape measured for FP32 and FP16 storage at
