@@ -606,12 +606,19 @@ __device__ __forceinline__ void setupTileGeom(const LolaPassProj *proj, int coun
     const double U = m[0] * X + m[3] * Y + m[6] * Z + m[9];
     const double V = m[1] * X + m[4] * Y + m[7] * Z + m[10];
     const double Wd = m[2] * X + m[5] * Y + m[8] * Z + m[11];
-    /* integer pixel offsets: floor(ix) = cu + floor(u'/w) on the paired path */
-    const float cu = rintf((float)U / (float)Wd);
-    const float cv = rintf((float)V / (float)Wd);
+    /* integer pixel offsets: floor(ix) = cu + floor(u'/w) on the paired path.
+       They are kept within one detector size of the padded image: where the
+       tile origin lies near the source plane (w ~ 0) its projection is huge,
+       and so would be the cancellation in u' = u - cu w for the tile's other
+       voxels.  Tiles that project inside (every fast tile) are unaffected. */
+    const float Wf = (float)g.width, Hf = (float)g.height, Mf = (float)g.margin;
+    float cu = rintf((float)U / (float)Wd);
+    float cv = rintf((float)V / (float)Wd);
+    cu = isfinite(cu) ? fminf(fmaxf(cu, -(Wf + Mf)), 2.0f * Wf + Mf) : 0.0f;
+    cv = isfinite(cv) ? fminf(fmaxf(cv, -(Hf + Mf)), 2.0f * Hf + Mf) : 0.0f;
     TileProj tp;
-    tp.cu = isfinite(cu) ? cu : 0.0f;
-    tp.cv = isfinite(cv) ? cv : 0.0f;
+    tp.cu = cu;
+    tp.cv = cv;
     tp.u0 = (float)(U - (double)tp.cu * Wd);
     tp.v0 = (float)(V - (double)tp.cv * Wd);
     tp.w0 = (float)Wd;

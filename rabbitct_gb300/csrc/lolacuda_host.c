@@ -862,10 +862,14 @@ static int launchPass(LolaCudaPlan *p, const double *mats, int count)
 int lolaCudaPlanBackprojectDevice(LolaCudaPlan *p, const float *d_images, size_t imageStride,
     const double *h_mats, int count)
 {
-  if (p == NULL || d_images == NULL || h_mats == NULL)
-    return setError("null argument");
+  if (p == NULL)
+    return setError("null plan");
   if (count < 0)
     return setError("negative projection count");
+  if (count == 0)
+    return 1;  /* nothing to read: the pointers may be null */
+  if (d_images == NULL || h_mats == NULL)
+    return setError("null argument");
   if (p->pending != 0)
     return setError("host-staged projections pending; synchronize the plan first");
   CUDA_TRY(cudaSetDevice(p->device));
@@ -917,7 +921,11 @@ static int stageHost(LolaCudaPlan *p, const float *image, const double *matrix, 
 int lolaCudaPlanBackprojectHost(LolaCudaPlan *p, const float *h_images, size_t imageStride,
     const double *h_mats, int count)
 {
-  if (p == NULL || h_images == NULL || h_mats == NULL)
+  if (p == NULL)
+    return setError("null plan");
+  if (count < 0)
+    return setError("negative projection count");
+  if (count > 0 && (h_images == NULL || h_mats == NULL))
     return setError("null argument");
   CUDA_TRY(cudaSetDevice(p->device));
   int flushed = 0;
