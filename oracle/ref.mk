@@ -10,6 +10,12 @@
 #                              analyseGeometry (computeLineRanges, shadow)
 #   oracle/_ref/rabbitRunner   the reference driver (src/rabbitRunner.c) with
 #                              its own registry, for end-to-end runs on .rct files
+#   oracle/_ref/rabbitRunnerLolaCUDA
+#                              the same driver and modules with the registry of
+#                              oracle/registry_lolacuda.c (the reference's table
+#                              plus a LolaCUDA row), linked to liblolacuda.so:
+#                              the drop-in as a maintainer would build it
+#                              (target `lolacuda`, needs the built library)
 #
 # The reference is plain C + one hand-written SIMD kernel; it is compiled with
 # its own flags (mk/include_GCC.mk: -O3 -ffast-math -march=native -std=c99,
@@ -59,7 +65,18 @@ $(OUT)/libref.so: $(addprefix $(SRC)/,$(LIB_SRC)) $(SRC)/$(KERNEL) | $(OUT)
 $(OUT)/rabbitRunner: $(addprefix $(SRC)/,$(RUN_SRC)) $(SRC)/$(KERNEL) | $(OUT)
 	$(CC) $(CFLAGS) -o $@ $(addprefix $(SRC)/,$(RUN_SRC)) $(SRC)/$(KERNEL) -lm
 
+LOLALIB ?= rabbitct_gb300/_lib
+REG_SRC := $(filter-out algorithmRegistry.c,$(RUN_SRC))
+
+lolacuda: $(OUT)/rabbitRunnerLolaCUDA
+
+$(OUT)/rabbitRunnerLolaCUDA: $(addprefix $(SRC)/,$(REG_SRC)) $(SRC)/$(KERNEL) \
+		oracle/registry_lolacuda.c $(LOLALIB)/liblolacuda.so | $(OUT)
+	$(CC) $(CFLAGS) -o $@ $(addprefix $(SRC)/,$(REG_SRC)) $(SRC)/$(KERNEL) \
+		oracle/registry_lolacuda.c -L$(LOLALIB) -llolacuda \
+		-Wl,-rpath,$(abspath $(LOLALIB)) -lm -lstdc++ -ldl -lpthread -lrt
+
 clean:
 	rm -rf $(OUT)
 
-.PHONY: all clean
+.PHONY: all clean lolacuda
