@@ -675,8 +675,10 @@ def run_batch(args, rank, world, local):
             "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (64 seeded phantoms and geometries)",
-            "config": {"workload": f"{len(specs)} uneven reconstructions, one persistent pass "
-                                   "per wave, graph-captured",
+            "config": {"workload": (f"{len(specs)} uneven reconstructions, graph-captured, "
+                                    + ("one persistent pass per wave"
+                                       if os.environ.get("LOLACUDA_BATCH_MODE", "0") == "1"
+                                       else "per-job passes in parallel graph branches")),
                        "storage": args.storage, "batch": args.batch,
                        "voxel_updates": updates, "generation_s": t_gen}}
     import ctypes as C

@@ -177,6 +177,7 @@ int launchBatchPack(const LolaBatchWave *w, cudaStream_t stream)
 {
   const dim3 block(32, 8);
   const dim3 grid((w->maxPitch + 31) / 32, (w->maxRows + 7) / 8, w->njobs * w->b);
+  (void)cudaGetLastError();  /* report this launch's error, not an earlier one */
   batchPackKernel<S><<<grid, block, 0, stream>>>(*w);
   return (int)cudaGetLastError();
 }
@@ -185,6 +186,7 @@ template <int S>
 int launchBatchPass(const LolaBatchWave *w, int blocks, cudaStream_t stream)
 {
   const dim3 block(32, 8);
+  (void)cudaGetLastError();  /* report this launch's error, not an earlier one */
   if (w->accumulation == LOLA_ACCUM_KAHAN)
     batchPassKernel<S, true><<<blocks, block, 0, stream>>>(*w);
   else

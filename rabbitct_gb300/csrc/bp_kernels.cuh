@@ -814,6 +814,7 @@ int launchPack(const LolaStoreDesc *st, const float *src, size_t srcStride, void
   a.rows = st->rows;
   const dim3 block(32, 8);
   const dim3 grid((st->pitch + 31) / 32, (st->rows + 7) / 8, count);
+  (void)cudaGetLastError();  /* report this launch's error, not an earlier one */
   packKernel<S><<<grid, block, 0, stream>>>(a);
   return (int)cudaGetLastError();
 }
@@ -825,6 +826,7 @@ int launchPassShape(const PassArgs &a, const LolaPassParams *P, cudaStream_t str
   const dim3 block(32, ROWS);
   const int nz = P->zEnd - P->zBegin;
   const dim3 grid((N + 31) / 32, (N + ROWS - 1) / ROWS, (nz + VPT - 1) / VPT);
+  (void)cudaGetLastError();
   passKernel<S, VPT, ROWS, KAHAN><<<grid, block, 0, stream>>>(a, *P);
   return (int)cudaGetLastError();
 }

@@ -418,6 +418,7 @@ int launchStagedShape(const PassArgs &a, const LolaPassParams *P, const StageArg
       (int)smem);
   if (e != cudaSuccess)
     return (int)e;
+  (void)cudaGetLastError();  /* report this launch's error, not an earlier one */
   kernel<<<grid, block, smem, stream>>>(a, *P, g, map);
   return (int)cudaGetLastError();
 }

@@ -94,6 +94,7 @@ void release(LolaCudaBatch *bt)
   do {                                                                                    \
     cudaError_t e_ = (call);                                                              \
     if (e_ != cudaSuccess) {                                                              \
+      (void)cudaGetLastError();                                                           \
       lolaSetError("batch: %s: %s", #call, cudaGetErrorString(e_));                       \
       return 0;                                                                           \
     }                                                                                     \

@@ -213,6 +213,7 @@ extern "C" int lolaCudaComputeLineRanges(const RabbitCtGlobalData *data, int16_t
     r.mm = data->voxelSize;
     r.o = data->O_Index;
     const dim3 grid((N + 255) / 256, N, nv);
+    (void)cudaGetLastError();  /* report this launch's error, not an earlier one */
     lineRangeKernel<<<grid, 256>>>(r);
     e = cudaGetLastError();
     for (int v = 0; e == cudaSuccess && v < nv; ++v)

@@ -55,11 +55,16 @@ int lolaSetError(const char *fmt, ...)
   return 0;
 }
 
+/* A failed call's error is also taken out of the runtime's last-error slot
+   (for the non-sticky ones, such as a failed allocation), so that a later
+   launch check does not report it again. */
 #define CUDA_TRY(call)                                                                   \
   do {                                                                                   \
     cudaError_t e_ = (call);                                                             \
-    if (e_ != cudaSuccess)                                                               \
+    if (e_ != cudaSuccess) {                                                             \
+      (void)cudaGetLastError();                                                          \
       return setError("%s:%d: %s: %s", __FILE__, __LINE__, #call, cudaGetErrorString(e_)); \
+    }                                                                                    \
   } while (0)
 
 #define LAUNCH_TRY(call)                                                                 \

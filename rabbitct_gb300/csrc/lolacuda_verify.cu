@@ -95,6 +95,7 @@ extern "C" int lolaCudaVerifyVolume(float *d_volume, size_t voxels, const uint16
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    (void)cudaGetLastError();  /* report this launch's error, not an earlier one */
     verifyKernel<<<sms * 8, 256, 0, st>>>(d_volume, d_ref, voxels, hus[0], hus[1],
         convertInPlace, d_out);
     e = cudaGetLastError();

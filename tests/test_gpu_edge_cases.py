@@ -1,7 +1,8 @@
 """Edge cases of the backprojection against the FP64 LolaBunny oracle: tiny
 and odd volume and detector sizes, a source inside the volume (w changes sign
 across it, so tiles take the clamped path with negative w), a ragged last
-pass at the largest batch, and calls without projections."""
+pass at the largest batch, calls without projections, the largest volume that
+fits (N=2048) and one that does not."""
 from __future__ import annotations
 
 import numpy as np
@@ -108,8 +109,6 @@ def test_ragged_last_pass_at_largest_batch(lib):
 def test_calls_without_projections(lib):
     """An empty host or device call and a module call of zero projections
     leave the volume as it was."""
-    import ctypes as C
-
     from rabbitct_gb300._native import check, config
     from rabbitct_gb300.lolacuda import GlobalData, Plan, module_functions
     scan = synth.make_scan(small_spec(nproj=2, width=64, height=48, seed=99))
@@ -130,3 +129,45 @@ def test_calls_without_projections(lib):
     check(iterate(gd.ref), "backprojection")
     check(finish(gd.ref), "finish")
     assert np.array_equal(vol, init)
+
+
+def test_largest_volume_n2048(lib):
+    """N=2048: a 32 GiB volume, 8.6e9 voxels (past 32-bit voxel indices), one
+    pass of two full-detector projections; three slices copied back and
+    sampled against the oracle."""
+    from rabbitct_gb300._native import check
+    from rabbitct_gb300.lolacuda import Plan
+    scan = synth.make_scan(synth.ScanSpec(nproj=2, seed=31))
+    n = 2048
+    vs = synth.voxel_size(n)
+    o = synth.origin_index(n, vs)
+    rng = np.random.default_rng(8)
+    area = n * n
+    with Plan(n, vs, o, scan.width, scan.height, storage="f32q", batch=2) as plan:
+        plan.zero()
+        plan.backproject_host(scan.images, scan.matrices)
+        plan.synchronize()
+        got, idx = [], []
+        for z in (0, n // 2 + 7, n - 1):
+            sl = np.empty(area, np.float32)
+            check(lib.lolaCudaCopyToHost(sl.ctypes.data, plan.volume_ptr + 4 * z * area,
+                                         sl.nbytes), "slice")
+            pick = rng.choice(area, 700, replace=False)
+            got.append(sl[pick])
+            idx.append(z * area + pick.astype(np.int64))
+    got = np.concatenate(got)
+    idx = np.concatenate(idx)
+    assert idx.max() > 2 ** 32
+    ref = oracle.bunny_points(n, vs, o, scan.matrices, scan.images, idx)
+    assert np.count_nonzero(ref) > 300
+    _close(got, ref, 1e-5)
+
+
+def test_volume_too_large_is_an_error(lib):
+    """A 2 TiB volume cannot be allocated: plan creation reports it."""
+    from rabbitct_gb300._native import LolaCudaError
+    from rabbitct_gb300.lolacuda import Plan
+    n = 8192
+    vs, o = _geom(n)
+    with pytest.raises(LolaCudaError):
+        Plan(n, vs, o, 64, 48)
