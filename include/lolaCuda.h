@@ -235,11 +235,15 @@ int lolaCudaPlanResetStats(LolaCudaPlan *plan);
 /* ---- Batched reconstructions ---------------------------------------------------
  * No counterpart in the reference, whose runner drives one reconstruction per
  * process.  Many volumes of uneven size, detector and projection count are
- * reconstructed together: waves of `batch` projections of every job, each
- * wave one pack launch and one persistent pass launch whose blocks pull
- * (job, tile) work items from a counter, the whole run captured into a CUDA
- * graph at create and replayed by each run.  All jobs share the config's
- * storage, accumulation and batch; FP32 arithmetic throughout. */
+ * reconstructed together, the whole run captured into a CUDA graph at create
+ * and replayed by each run.  Two schedules (config batchMode):
+ * LOLA_BATCH_BRANCHES (default) runs each job's pack and pass launches in one
+ * of batchBranches parallel graph branches, with tile shapes timed per
+ * (N, detector) class when batchTune is set; LOLA_BATCH_PERSISTENT runs, per
+ * wave of `batch` projections of every job, one pack launch and one
+ * persistent pass launch whose blocks pull (job, tile) work items from a
+ * counter.  All jobs share the config's storage, accumulation and batch; FP32
+ * arithmetic throughout. */
 typedef struct {
   LolaCudaGeometry geometry;   /* whole volume: slice fields must be 0 */
   int32_t projections;

@@ -2,11 +2,15 @@
  * projection count, reconstructed together (host side of bp_batch.cuh).
  *
  * lolaCudaBatchCreate lays out one projection ring holding `b` stored slots
- * per job, the per-wave projection parameters of every job, and per-wave
- * work lists (prefix sums of the tiles of the jobs that still have
- * projections in that wave), then captures the whole run — a counter reset,
- * and per wave one pack launch and one persistent pass launch — into a CUDA
- * graph.  lolaCudaBatchRun replays the graph on the batch's stream.
+ * per job and captures the whole run into a CUDA graph; lolaCudaBatchRun
+ * replays the graph on the batch's stream.  Two schedules:
+ *  - branches (default): each job's pack and pass launches (the plan kernels,
+ *    with a tile shape timed per (N, detector) class when batchTune is set)
+ *    go to one of K parallel graph branches, largest jobs first;
+ *  - persistent: per-wave projection parameters and work lists (prefix sums
+ *    of the tiles of the jobs that still have projections in that wave), then
+ *    a counter reset and, per wave, one pack launch and one persistent pass
+ *    launch (bp_batch.cuh).
  */
 #include <stdint.h>
 #include <stdlib.h>

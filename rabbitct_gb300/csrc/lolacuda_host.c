@@ -111,7 +111,7 @@ void lolaCudaDefaultConfig(LolaCudaConfig *c)
   c->accumulation = LOLA_ACCUM_PLAIN;
   c->batch = 16;
   /* 16 x 4 tiles: the fastest shape measured for FP32 and FP16 storage at
-     N=1024 on GB300 (f32 1151, f16qx 1337 GUPS vs 1026 and 1224 for 8 x 8) */
+     N=1024 on GB300 (f32 1151, f16qx 1337 GUPS vs 1026 and 1224 for 8x8 tiles) */
   c->voxelsPerThread = 16;
   c->rowsPerBlock = 4;
   c->syncEachCall = 1;
