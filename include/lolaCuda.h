@@ -123,7 +123,8 @@ typedef struct {
   int32_t batchBranches; /* LOLA_BATCH_BRANCHES: concurrent graph branches (0 = 16) */
   int32_t batchTune;     /* LOLA_BATCH_BRANCHES: time the tile shapes once per distinct
                             (N, detector) class at create and use the fastest for
-                            its jobs (1), or use voxelsPerThread x rowsPerBlock (0) */
+                            its jobs (1), or use voxelsPerThread x rowsPerBlock (0,
+                            the default) */
   int32_t reserved[3];
 } LolaCudaConfig;
 

@@ -7,7 +7,8 @@
  * work items — (job, tile) pairs, numbered job by job — from an atomic
  * counter until the wave is done, so small and large jobs balance across the
  * SMs without one launch per job.  A work item is exactly a passKernel tile
- * (32 x 8 x 8 voxels in registers across the wave's projections).  The host
+ * of 8 rows of 8 voxels per thread (LOLA_WARP_X x 256 / LOLA_WARP_X x 8
+ * voxels, in registers across the wave's projections).  The host
  * captures the whole sequence of waves into a CUDA graph once and replays it.
  */
 #pragma once
@@ -73,13 +74,15 @@ template <int S, bool KAHAN>
 __global__ void __launch_bounds__(256, LOLA_BATCH_MIN_BLOCKS) batchPassKernel(const LolaBatchWave w)
 {
   constexpr int VPT = 8, ROWS = 8;
+  constexpr int TX = LOLA_WARP_X, TY = 32 * ROWS / TX;
   __shared__ TileProj sp[LOLA_MAX_BATCH];
   /* the current work item: its job's descriptor and tile, shared by the
      block so the per-voxel loop keeps only what passKernel keeps */
   __shared__ LolaBatchJob J;
   __shared__ int itemJob, itemCount, itemX0, itemY0, itemZ0, itemDone;
   const int tid = threadIdx.y * 32 + threadIdx.x;
-  const float fi = (float)threadIdx.x, fj = (float)threadIdx.y;
+  const int tx = threadIdx.x % TX, ty = threadIdx.y * (32 / TX) + threadIdx.x / TX;
+  const float fi = (float)tx, fj = (float)ty;
   for (;;) {
     if (tid == 0) {
       const long long item = atomicAdd(w.counter, 1);
@@ -98,9 +101,9 @@ __global__ void __launch_bounds__(256, LOLA_BATCH_MIN_BLOCKS) batchPassKernel(co
         long long t = item - w.tilePrefix[lo];
         itemJob = lo;
         itemCount = min(w.b, J.nproj - w.wave * w.b);
-        itemX0 = (int)(t % J.tilesX) * 32;
+        itemX0 = (int)(t % J.tilesX) * TX;
         t /= J.tilesX;
-        itemY0 = (int)(t % J.tilesY) * ROWS;
+        itemY0 = (int)(t % J.tilesY) * TY;
         itemZ0 = (int)(t / J.tilesY) * VPT;
       }
     }
@@ -118,10 +121,10 @@ __global__ void __launch_bounds__(256, LOLA_BATCH_MIN_BLOCKS) batchPassKernel(co
       g.width = J.width;
       g.height = J.height;
       g.margin = J.margin;
-      setupTileGeom<ROWS, VPT>(w.proj + (size_t)itemJob * w.b, count, g, sp, tid, 32 * ROWS,
+      setupTileGeom<ROWS, VPT, TX>(w.proj + (size_t)itemJob * w.b, count, g, sp, tid, 32 * ROWS,
           x0, y0, z0);
       const int N = J.N;
-      const int x = x0 + threadIdx.x, y = y0 + threadIdx.y;
+      const int x = x0 + tx, y = y0 + ty;
       const bool inXY = (x < N) && (y < N);
       const size_t slice = (size_t)N * (size_t)N;
       float2 acc[VPT / 2], comp[VPT / 2];

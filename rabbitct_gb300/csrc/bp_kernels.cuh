@@ -11,8 +11,10 @@
  * for u in (-2, 0)) and reads 0 outside the detector (src/LolaBunny.c:11-30).
  *
  * GB300 mapping:
- *  - A CTA owns a tile of 32 (x) x ROWS (y) x VPT (z) voxels.  Each thread
- *    keeps its VPT voxels (one x column, consecutive z) in registers for a
+ *  - A CTA of ROWS warps owns a tile of 32 ROWS x VPT voxels: each warp an
+ *    LOLA_WARP_X x (32 / LOLA_WARP_X) patch of the xy plane (8 x 4 by default,
+ *    a compact detector footprint), each thread VPT voxels along z.  Each
+ *    thread keeps its VPT voxels (one xy column, consecutive z) in registers for a
  *    whole pass of up to LOLA_MAX_BATCH projections, so the volume crosses HBM
  *    once per pass instead of once per projection.
  *  - Per (tile, projection) the tile origin is projected in FP64 (the only
@@ -592,7 +594,7 @@ struct TileGeom {
   int width, height, margin;
 };
 
-template <int ROWS, int VPT>
+template <int ROWS, int VPT, int TX = 32>
 __device__ __forceinline__ void setupTileGeom(const LolaPassProj *proj, int count,
     const TileGeom &g, TileProj *sp, int tid, int nthreads, int x0, int y0, int z0)
 {
@@ -636,7 +638,8 @@ __device__ __forceinline__ void setupTileGeom(const LolaPassProj *proj, int coun
   __syncthreads();
 
   /* -- setup B: footprint of the tile from its 8 corners, 8 lanes per view -- */
-  const int ex = min(32, N - x0) - 1, ey = min(ROWS, N - y0) - 1;
+  /* tile: TX x (32 ROWS / TX) x VPT voxels */
+  const int ex = min(TX, N - x0) - 1, ey = min(32 * ROWS / TX, N - y0) - 1;
   const int ez = min(VPT, g.zEnd - z0) - 1;
   for (int base = 0; base < 8 * count; base += nthreads) {
     const int t = base + tid;
@@ -688,7 +691,7 @@ __device__ __forceinline__ void setupTileGeom(const LolaPassProj *proj, int coun
 
 }
 
-template <int ROWS, int VPT>
+template <int ROWS, int VPT, int TX = 32>
 __device__ __forceinline__ void setupTile(const LolaPassParams &P, const PassArgs &a,
     TileProj *sp, int tid, int nthreads, int x0, int y0, int z0)
 {
@@ -700,7 +703,7 @@ __device__ __forceinline__ void setupTile(const LolaPassParams &P, const PassArg
   g.width = a.width;
   g.height = a.height;
   g.margin = a.margin;
-  setupTileGeom<ROWS, VPT>(P.proj, P.count, g, sp, tid, nthreads, x0, y0, z0);
+  setupTileGeom<ROWS, VPT, TX>(P.proj, P.count, g, sp, tid, nthreads, x0, y0, z0);
 }
 
 /* Resident blocks per SM requested from the register allocator.  The pass is
@@ -731,11 +734,13 @@ __global__ void __launch_bounds__(32 * ROWS, LOLA_PASS_MIN_BLOCKS(S, VPT, ROWS))
 {
   __shared__ TileProj sp[LOLA_MAX_BATCH];
   const int N = P.N;
-  const int x0 = blockIdx.x * 32, y0 = blockIdx.y * ROWS, z0 = P.zBegin + blockIdx.z * VPT;
+  /* a warp covers TX x (32 / TX) voxels of the xy plane */
+  constexpr int TX = LOLA_WARP_X, TY = 32 * ROWS / TX;
+  const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY, z0 = P.zBegin + blockIdx.z * VPT;
   const int tid = threadIdx.y * 32 + threadIdx.x;
   const int count = P.count;
 
-  setupTile<ROWS, VPT>(P, a, sp, tid, 32 * ROWS, x0, y0, z0);
+  setupTile<ROWS, VPT, TX>(P, a, sp, tid, 32 * ROWS, x0, y0, z0);
 
   if (a.tileCounters != nullptr && tid == 0) {
     unsigned long long nSkip = 0, nFast = 0, nSlow = 0, nPaired = 0;
@@ -753,7 +758,8 @@ __global__ void __launch_bounds__(32 * ROWS, LOLA_PASS_MIN_BLOCKS(S, VPT, ROWS))
   }
 
   /* -- main: voxels in registers across the pass -- */
-  const int x = x0 + threadIdx.x, y = y0 + threadIdx.y;
+  const int tx = threadIdx.x % TX, ty = threadIdx.y * (32 / TX) + threadIdx.x / TX;
+  const int x = x0 + tx, y = y0 + ty;
   const bool inXY = (x < N) && (y < N);
   const size_t slice = (size_t)N * (size_t)N;
   /* the plan holds only the slab z in [zBegin, zEnd); the column address is
@@ -771,7 +777,7 @@ __global__ void __launch_bounds__(32 * ROWS, LOLA_PASS_MIN_BLOCKS(S, VPT, ROWS))
       voxel(comp, k) = 0.0f;
     }
   }
-  const float fi = (float)threadIdx.x, fj = (float)threadIdx.y;
+  const float fi = (float)tx, fj = (float)ty;
   for (int p = 0; p < count; ++p) {
     const int mode = sp[p].mode;
     if (mode == MODE_SKIP)
@@ -825,7 +831,8 @@ int launchPassShape(const PassArgs &a, const LolaPassParams *P, cudaStream_t str
   const int N = P->N;
   const dim3 block(32, ROWS);
   const int nz = P->zEnd - P->zBegin;
-  const dim3 grid((N + 31) / 32, (N + ROWS - 1) / ROWS, (nz + VPT - 1) / VPT);
+  constexpr int TX = LOLA_WARP_X, TY = 32 * ROWS / TX;
+  const dim3 grid((N + TX - 1) / TX, (N + TY - 1) / TY, (nz + VPT - 1) / VPT);
   (void)cudaGetLastError();
   passKernel<S, VPT, ROWS, KAHAN><<<grid, block, 0, stream>>>(a, *P);
   return (int)cudaGetLastError();

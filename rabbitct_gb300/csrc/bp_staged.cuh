@@ -9,7 +9,7 @@
  * memory.  The L2 round trip of every first touch, which dominated the
  * load-path kernel's stalls, leaves the critical path.
  *
- * Block: ROWS consumer warps (32 x ROWS x VPT voxel tile, voxels in registers
+ * Block: ROWS consumer warps (the passKernel tile of 32 ROWS x VPT voxels, in registers
  * across the pass) plus one producer warp.  Barriers per stage s:
  *   full[s]   1 arrival (producer, with the box's byte count), completed by
  *             the tensor copy;
@@ -273,7 +273,8 @@ __global__ void __launch_bounds__(32 * (ROWS + 1), LOLA_STAGED_MIN_BLOCKS)
   __shared__ __align__(8) unsigned long long bars[2 * NS]; /* full[NS], empty[NS] */
   const int N = P.N;
   const int count = P.count;
-  const int x0 = blockIdx.x * 32, y0 = blockIdx.y * ROWS, z0 = P.zBegin + blockIdx.z * VPT;
+  constexpr int TX = LOLA_WARP_X, TY = 32 * ROWS / TX;
+  const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY, z0 = P.zBegin + blockIdx.z * VPT;
   const int tid = threadIdx.y * 32 + threadIdx.x;
   const uint32_t full0 = smemAddr(&bars[0]);
   const uint32_t empty0 = smemAddr(&bars[NS]);
@@ -286,7 +287,7 @@ __global__ void __launch_bounds__(32 * (ROWS + 1), LOLA_STAGED_MIN_BLOCKS)
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   }
-  setupTile<ROWS, VPT>(P, a, sp, tid, 32 * (ROWS + 1), x0, y0, z0);
+  setupTile<ROWS, VPT, TX>(P, a, sp, tid, 32 * (ROWS + 1), x0, y0, z0);
 
   /* which fast-path projections fit the box: numbered in pass order */
   if (tid == 0) {
@@ -352,7 +353,8 @@ __global__ void __launch_bounds__(32 * (ROWS + 1), LOLA_STAGED_MIN_BLOCKS)
   }
 
   /* consumer warps */
-  const int x = x0 + threadIdx.x, y = y0 + threadIdx.y;
+  const int tx = threadIdx.x % TX, ty = threadIdx.y * (32 / TX) + threadIdx.x / TX;
+  const int x = x0 + tx, y = y0 + ty;
   const bool inXY = (x < N) && (y < N);
   const size_t slice = (size_t)N * (size_t)N;
   /* the plan holds only the slab z in [zBegin, zEnd) */
@@ -364,7 +366,7 @@ __global__ void __launch_bounds__(32 * (ROWS + 1), LOLA_STAGED_MIN_BLOCKS)
     voxel(acc, k) = (inXY && z0 + k < P.zEnd) ? vcol[k * slice] : 0.0f;
     voxel(comp, k) = 0.0f;
   }
-  const float fi = (float)threadIdx.x, fj = (float)threadIdx.y;
+  const float fi = (float)tx, fj = (float)ty;
   bool abandoned = false;
   for (int p = 0; p < count; ++p) {
     const int mode = sp[p].mode;
@@ -411,7 +413,8 @@ int launchStagedShape(const PassArgs &a, const LolaPassParams *P, const StageArg
   const int N = P->N;
   const dim3 block(32, ROWS + 1);
   const int nz = P->zEnd - P->zBegin;
-  const dim3 grid((N + 31) / 32, (N + ROWS - 1) / ROWS, (nz + VPT - 1) / VPT);
+  constexpr int TX = LOLA_WARP_X, TY = 32 * ROWS / TX;
+  const dim3 grid((N + TX - 1) / TX, (N + TY - 1) / TY, (nz + VPT - 1) / VPT);
   const size_t smem = (size_t)LOLA_STAGES * (size_t)g.stageBytes;
   auto kernel = stagedPassKernel<S, VPT, ROWS, KAHAN>;
   cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,

@@ -282,8 +282,9 @@ int build(LolaCudaBatch *bt, const LolaCudaJob *jobs)
     J.slotBytes = J.slotElems * pix;
     J.voxelSize = g.voxelSize;
     J.originIndex = g.originIndex;
-    J.tilesX = (J.N + 31) / 32;
-    J.tilesY = (J.N + 7) / 8;
+    /* the persistent pass's tiles: LOLA_WARP_X x (256 / LOLA_WARP_X) x 8 */
+    J.tilesX = (J.N + LOLA_WARP_X - 1) / LOLA_WARP_X;
+    J.tilesY = (J.N + 256 / LOLA_WARP_X - 1) / (256 / LOLA_WARP_X);
     J.tilesZ = (J.N + 7) / 8;
     J.nproj = jobs[j].projections;
     J.volume = jobs[j].d_volume;

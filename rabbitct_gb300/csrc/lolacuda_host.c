@@ -132,7 +132,9 @@ void lolaCudaDefaultConfig(LolaCudaConfig *c)
   c->staging = envInt("LOLACUDA_STAGING", 0);
   c->batchMode = envInt("LOLACUDA_BATCH_MODE", LOLA_BATCH_BRANCHES);
   c->batchBranches = envInt("LOLACUDA_BATCH_BRANCHES", 16);
-  c->batchTune = envInt("LOLACUDA_BATCH_TUNE", 1);
+  /* per-class shape tuning measured no better than the default 16 x 4 tiles on
+     the 64-job uneven workload (912 vs 921 GUPS), so it is opt-in */
+  c->batchTune = envInt("LOLACUDA_BATCH_TUNE", 0);
 }
 
 static int validateConfig(const LolaCudaConfig *c)
