@@ -10,16 +10,25 @@ every projection, clipped or not).
 Lines printed (rank 0, one JSON object):
   value   device-resident throughput of the FP16-stored path (projections
           already in HBM when the timed region starts; CUDA events on the
-          plan's stream); the FP32 path is measured the same way beside it
+          plan's stream); tile shape, batch and staging are picked by the
+          autotuner on the first 32 projections before the timed region
+  fp32_path, fp32_quads  the plain FP32 path (four FP32 taps per update) and
+          FP32 storage as 2x2 quads (the same results), measured the same way
   e2e     the same metric through the RabbitCT module API (prepare, one
           backprojection call per projection from pinned host buffers,
-          finish with the volume copied back), wall clock around the calls
+          finish with the volume copied back), wall clock around the calls,
+          median of --e2e-steps
   roofline  the pass kernel against the measured gather and FP32-issue
-          ceilings (probe kernels run on the same GPU), plus its HBM view
+          ceilings (probe kernels run on the same GPU), the DRAM bytes of one
+          launch from the committed ncu capture of the same configuration,
+          plus its HBM view
+  clocks  SM clocks and throttle reasons sampled during the timed region
   cpu_baseline  the LolaOPT port (oracle/oracle_opt.c) on the host cores,
-          on a bounded sample of the same workload
+          on a bounded sample of the same workload (warm repeat)
 `--impl reference` times the reference's CPU method alone (the LolaOPT port;
 the reference's own build cannot travel to this host) on the same workload.
+`--workload batch64` runs 64 uneven reconstructions as one batch against the
+same jobs through sequential plain FP32 plans.
 """
 from __future__ import annotations
 
