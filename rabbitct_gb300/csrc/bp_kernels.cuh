@@ -341,7 +341,19 @@ struct PackArgs {
   size_t slotElems;
   int slot0;
   int width, height, margin, pitch, rows;
+  unsigned long long surf[LOLA_MAX_BATCH];  /* per ring slot, or 0 (LolaStoreDesc) */
 };
+
+/* Copies a stored pixel into a texture layout's CUDA array as well. */
+template <class E>
+__device__ __forceinline__ void surfStore(unsigned long long surf, E e, int x, int y)
+{
+  surf2Dwrite(e, (cudaSurfaceObject_t)surf, x * (int)sizeof(E), y);
+}
+__device__ __forceinline__ void surfStore(unsigned long long surf, __half e, int x, int y)
+{
+  surf2Dwrite(__half_as_ushort(e), (cudaSurfaceObject_t)surf, x * 2, y);
+}
 
 template <int S>
 __global__ void __launch_bounds__(256) packKernel(const PackArgs a)
@@ -363,6 +375,11 @@ __global__ void __launch_bounds__(256) packKernel(const PackArgs a)
     Layout<S>::store(a.ring, o, px(u, v), px(u + 1, v), px(u, v + 1), px(u + 1, v + 1));
   else
     Layout<S>::store(a.ring, o, px(u, v), 0.f, 0.f, 0.f);
+  if constexpr (Layout<S>::kTex || Layout<S>::kMixed) {
+    const unsigned long long surf = a.surf[a.slot0 + p];
+    if (surf)  /* the same element, read back from this thread's own store */
+      surfStore(surf, static_cast<const typename Layout<S>::Elem *>(a.ring)[o], pu, pv);
+  }
 }
 
 /* ---- backprojection pass ---------------------------------------------------- */
@@ -818,6 +835,8 @@ int launchPack(const LolaStoreDesc *st, const float *src, size_t srcStride, void
   a.margin = st->margin;
   a.pitch = st->pitch;
   a.rows = st->rows;
+  for (int i = 0; i < LOLA_MAX_BATCH; ++i)
+    a.surf[i] = st->surfObjects[i];
   const dim3 block(32, 8);
   const dim3 grid((st->pitch + 31) / 32, (st->rows + 7) / 8, count);
   (void)cudaGetLastError();  /* report this launch's error, not an earlier one */

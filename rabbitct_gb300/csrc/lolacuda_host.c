@@ -193,6 +193,7 @@ struct LolaCudaPlan {
   cudaEvent_t timerStart, timerStop;
   float *d_volume;
   void *d_ring;
+  cudaArray_t texArrays[LOLA_MAX_BATCH];  /* texture layouts with LOLA_TEX_ARRAYS */
   float *d_stage;
   unsigned long long *d_counters;
   int *d_error;           /* staged-pass wait timeouts */
@@ -266,9 +267,14 @@ static int planRelease(LolaCudaPlan *p)
     cudaEventDestroy(p->events[i].stop);
   }
   free(p->events);
-  for (int i = 0; i < LOLA_MAX_BATCH; i++)
+  for (int i = 0; i < LOLA_MAX_BATCH; i++) {
     if (p->store.texObjects[i])
       cudaDestroyTextureObject((cudaTextureObject_t)p->store.texObjects[i]);
+    if (p->store.surfObjects[i])
+      cudaDestroySurfaceObject((cudaSurfaceObject_t)p->store.surfObjects[i]);
+    if (p->texArrays[i])
+      cudaFreeArray(p->texArrays[i]);
+  }
   cudaFree(p->d_volume);
   cudaFree(p->d_ring);
   cudaFree(p->d_stage);
@@ -362,6 +368,18 @@ static int planInit(LolaCudaPlan *p)
       rd.res.pitch2D.width = (size_t)s->pitch;
       rd.res.pitch2D.height = (size_t)s->rows;
       rd.res.pitch2D.pitchInBytes = (size_t)s->pitch * s->elemBytes;
+      if (LOLA_TEX_ARRAYS) {
+        /* a CUDA array per slot (block-linear), written through a surface */
+        const struct cudaChannelFormatDesc cd = rd.res.pitch2D.desc;
+        CUDA_TRY(cudaMallocArray(&p->texArrays[i], &cd, (size_t)s->pitch, (size_t)s->rows,
+            cudaArraySurfaceLoadStore));
+        memset(&rd, 0, sizeof(rd));
+        rd.resType = cudaResourceTypeArray;
+        rd.res.array.array = p->texArrays[i];
+        cudaSurfaceObject_t sf = 0;
+        CUDA_TRY(cudaCreateSurfaceObject(&sf, &rd));
+        s->surfObjects[i] = (unsigned long long)sf;
+      }
       struct cudaTextureDesc td;
       memset(&td, 0, sizeof(td));
       td.addressMode[0] = cudaAddressModeBorder;

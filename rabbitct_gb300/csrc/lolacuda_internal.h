@@ -35,7 +35,20 @@ typedef struct {
   size_t slotElems;     /* pixels per ring slot (>= pitch * rows, 256 B multiple) */
   /* texture layouts: one texture object per ring slot (cudaTextureObject_t) */
   unsigned long long texObjects[LOLA_MAX_BATCH];
+  /* texture layouts read from CUDA arrays: the surface object (cudaSurfaceObject_t)
+     the pack kernel writes each slot's array through; 0 = textures read the
+     linear ring */
+  unsigned long long surfObjects[LOLA_MAX_BATCH];
 } LolaStoreDesc;
+
+/* 1: the plan's texture layouts read CUDA arrays (the GPU's block-linear 2D
+   layout) written by the pack kernel through surfaces; 0: pitch-linear
+   textures over the ring.  Measured on GB300 at N=1024 the arrays gain
+   nothing (tex16 +0.5 %, tex32 0, f16qx -2.5 % for its second copy): the
+   footprints are small enough for the texture cache either way. */
+#ifndef LOLA_TEX_ARRAYS
+#define LOLA_TEX_ARRAYS 0
+#endif
 
 /* One projection of a kernel pass: the FP64 matrix and its FP32 voxel steps. */
 typedef struct {

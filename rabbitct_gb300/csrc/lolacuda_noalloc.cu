@@ -105,6 +105,7 @@ extern "C" int lolaCudaBackprojectNoAlloc(const LolaCudaGeometry *g, const LolaC
     return lolaSetError("null argument");
 
   LolaStoreDesc st;
+  memset(&st, 0, sizeof(st));  /* no texture objects or surfaces */
   st.storage = c.storage;
   st.elemBytes = eb;
   st.margin = LOLA_MARGIN;
