@@ -323,7 +323,10 @@ def my_slab(args, dist):
     """z-slab of this rank: all of the volume unless sharding by slabs."""
     from rabbitct_gb300.lolacuda import slab
     if args.shard == "slabs" and dist.world > 1:
-        return slab(args.n, dist.rank, dist.world, args.vpt)
+        # aligned to 16 slices, a multiple of every tile depth (4, 8, 16): the
+        # slabs stay on tile boundaries whatever shape each rank's autotuner
+        # picks, so ranks agree on them and the union equals one whole volume
+        return slab(args.n, dist.rank, dist.world, 16)
     return (0, args.n)
 
 

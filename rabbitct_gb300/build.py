@@ -49,6 +49,24 @@ def _run(cmd: list[str]) -> None:
                            f"{proc.stdout}\n{proc.stderr}")
 
 
+class _BuildLock:
+    """Serialises builds of this tree across processes (one process per GPU
+    may start at once, each checking the library), so that no two compile
+    into the same outputs."""
+
+    def __enter__(self):
+        import fcntl
+        OBJ.mkdir(parents=True, exist_ok=True)
+        self._f = open(OBJ / ".build.lock", "w")
+        fcntl.flock(self._f, fcntl.LOCK_EX)
+        return self
+
+    def __exit__(self, *exc):
+        import fcntl
+        fcntl.flock(self._f, fcntl.LOCK_UN)
+        self._f.close()
+
+
 def _stale(target: Path, deps: list[Path]) -> bool:
     if not target.exists():
         return True
@@ -56,17 +74,19 @@ def _stale(target: Path, deps: list[Path]) -> bool:
     return any(d.stat().st_mtime > t for d in deps)
 
 
-def build_synth(force: bool = False) -> Path:
+def _build_synth(force: bool = False) -> Path:
     LIB.mkdir(exist_ok=True)
     out = LIB / "librctsynth.so"
     src = CSRC / "rct_synth.c"
     if force or _stale(out, [src]):
+        tmp = out.with_suffix(".so.tmp")
         _run(["gcc", "-O2", "-fno-fast-math", "-ffp-contract=off", "-std=c99", "-fopenmp",
-              "-fPIC", "-shared", "-o", str(out), str(src), "-lm"])
+              "-fPIC", "-shared", "-o", str(tmp), str(src), "-lm"])
+        os.replace(tmp, out)
     return out
 
 
-def build_lolacuda(force: bool = False, jobs: int | None = None) -> Path:
+def _build_lolacuda(force: bool = False, jobs: int | None = None) -> Path:
     LIB.mkdir(exist_ok=True)
     OBJ.mkdir(exist_ok=True)
     cuda = _cuda_home()
@@ -107,11 +127,15 @@ def build_lolacuda(force: bool = False, jobs: int | None = None) -> Path:
         futs += [ex.submit(compile_c, n) for n in C_SOURCES]
         objs = [f.result() for f in futs]
     if force or _stale(out, objs):
-        _run([nvcc, *ARCH, "-shared", "-o", str(out), *map(str, objs), "-cudart", "static"])
+        # linked under another name and renamed: a process that has the old
+        # library mapped keeps a whole file
+        tmp = out.with_suffix(".so.tmp")
+        _run([nvcc, *ARCH, "-shared", "-o", str(tmp), *map(str, objs), "-cudart", "static"])
+        os.replace(tmp, out)
     return out
 
 
-def build_oracle(force: bool = False) -> Path:
+def _build_oracle(force: bool = False) -> Path:
     """Builds the oracle (test infrastructure) and, where the reference sources
     are present, the reference itself into oracle/_ref."""
     oracle = REPO / "oracle"
@@ -124,10 +148,31 @@ def build_oracle(force: bool = False) -> Path:
     return oracle / "liboracle.so"
 
 
+def build_synth(force: bool = False) -> Path:
+    """The synthetic-scan generator, librctsynth.so."""
+    with _BuildLock():
+        return _build_synth(force)
+
+
+def build_lolacuda(force: bool = False, jobs: int | None = None) -> Path:
+    """liblolacuda.so: every CUDA translation unit for sm_103a plus the C host
+    code, compiled in parallel; only stale objects are rebuilt."""
+    with _BuildLock():
+        return _build_lolacuda(force, jobs)
+
+
+def build_oracle(force: bool = False) -> Path:
+    """The oracle (test infrastructure) and, where the reference sources are
+    present, the reference itself into oracle/_ref."""
+    with _BuildLock():
+        return _build_oracle(force)
+
+
 def build_all(force: bool = False) -> None:
-    build_synth(force)
-    build_lolacuda(force)
-    build_oracle(force)
+    with _BuildLock():
+        _build_synth(force)
+        _build_lolacuda(force)
+        _build_oracle(force)
 
 
 if __name__ == "__main__":
