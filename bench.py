@@ -107,8 +107,9 @@ def parse_args():
                     help="n1024: one N=1024 reconstruction (headline); batch64: 64 uneven "
                          "reconstructions in one graph-captured persistent run")
     ap.add_argument("--jobs", type=int, default=64, help="batch64: number of reconstructions")
-    ap.add_argument("--n", type=int, default=1024)
-    ap.add_argument("--nproj", type=int, default=496)
+    # long aliases: under torchrun, whose own parser prefix-matches --n*
+    ap.add_argument("--n", "--problem-size", dest="n", type=int, default=1024)
+    ap.add_argument("--nproj", "--projections", dest="nproj", type=int, default=496)
     ap.add_argument("--width", type=int, default=1248)
     ap.add_argument("--height", type=int, default=960)
     ap.add_argument("--storage", default="f16qx", choices=list(STORAGE_IDS))
