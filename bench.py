@@ -494,8 +494,8 @@ def time_e2e(args, dist, scan, vs, o, storage) -> dict:
         return time_e2e_slab(args, dist, scan, vs, o, storage)
     import ctypes as C
 
-    from rabbitct_gb300._native import check, config, load_lolacuda
-    from rabbitct_gb300.lolacuda import GlobalData, module_functions
+    from rabbitct_gb300._native import LolaCudaScanTiming, check, config, load_lolacuda
+    from rabbitct_gb300.lolacuda import GlobalData
     lib = load_lolacuda()
     n, W, H = args.n, scan.width, scan.height
     nbytes_vol = 4 * n ** 3
@@ -516,26 +516,22 @@ def time_e2e(args, dist, scan, vs, o, storage) -> dict:
                                        voxels_per_thread=args.vpt, rows_per_block=args.rows,
                                        exit_on_error=0, staging=args.staging,
                                        sync_each_call=0)), "config")
-    prepare, iterate, finish = module_functions(lib, "lolaCuda")
-    times = []
+    times, phases = [], []
     for step in range(1 + args.e2e_steps):
         vol.fill(0.0)  # the runner hands over a zeroed volume (src/rabbitRunner.c:192)
         gd = GlobalData(n, vs, o, W, H, 1, volume=vol, geometry=mats)
+        timing = LolaCudaScanTiming()
         dist.barrier()
-        t0 = time.perf_counter()
-        check(prepare(gd.ref), "prepare")
-        gd.data.numberOfProjections = 1
-        for p in range(scan.nproj):
-            # a zero-copy reader: the projection buffer points at the pinned image
-            gd.projs[0].id = p + 1
-            gd.projs[0].matrix = mats[p].ctypes.data_as(C.POINTER(C.c_double))
-            gd.projs[0].image = C.cast(hi + p * 4 * W * H, C.POINTER(C.c_float))
-            check(iterate(gd.ref), "backprojection")
-        check(finish(gd.ref), "finish")
-        dt = time.perf_counter() - t0
+        # the runner's loop in C (lolaCudaRunScan): prepare, one backprojection
+        # call per projection from the pinned images (-b 1, ids 1..496, -a),
+        # finish; wall clock from prepare to the volume back in host memory
+        check(lib.lolaCudaRunScan(gd.ref, hi, W * H, mats.ctypes.data, scan.nproj, 1,
+                                  C.byref(timing)), "run scan")
+        dt = timing.totalSeconds
         dist.barrier()
         if step > 0:
             times.append(dist.max(dt))
+            phases.append((timing.prepareSeconds, timing.callSeconds, timing.finishSeconds))
     checksum = float(np.float64(vol[n // 2].sum()))
     lib.lolaCudaHostFree(hv)
     lib.lolaCudaHostFree(hi)
@@ -544,9 +540,13 @@ def time_e2e(args, dist, scan, vs, o, storage) -> dict:
     return {"value": gups, "unit": "GUPS", "seconds": t,
             "h2d_bytes_per_step": nbytes_vol + nbytes_img,
             "d2h_bytes_per_step": nbytes_vol,
-            "path": "module API, -b 1 -a calls, pinned host, syncEachCall 0; volume upload "
-                    "and download overlapped with the first and last pass",
-            "checksum_mid_slice": checksum}
+            "path": "module API driven by a C loop (lolaCudaRunScan): -b 1 -a calls, pinned "
+                    "host, syncEachCall 0; volume upload and download overlapped with the first "
+                    "and last pass",
+            "checksum_mid_slice": checksum,
+            "phases_ms": {"prepare": 1e3 * statistics.median(p[0] for p in phases),
+                          "calls": 1e3 * statistics.median(p[1] for p in phases),
+                          "finish": 1e3 * statistics.median(p[2] for p in phases)}}
 
 
 def run_gpu(args, rank, world, local):

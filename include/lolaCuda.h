@@ -368,6 +368,25 @@ int lolaCudaReconstructFile(const char *path, int problemSize, float voxelSize,
     float originIndex, const LolaCudaConfig *config, float *h_volume,
     LolaCudaFileReport *report);
 
+/* The runner's module loop (src/rabbitRunner.c:222-287) over projections that
+ * are already in host memory, in C: prepare, one lolaCudaBackprojection call
+ * per callBatch projections (each Projection pointing into h_images and
+ * h_matrices, ids 1..count), finish.  data holds the geometry, volumeData and
+ * (optionally, like -a) globalGeometry with numberOfProjections = count; its
+ * projectionBuffer and numberOfProjections are used during the calls and
+ * restored.  Wall-clock times of the three phases (CLOCK_MONOTONIC), like the
+ * runner's timer around its calls.  No counterpart in the reference, whose
+ * runner reads each projection from the file between calls. */
+typedef struct {
+  double prepareSeconds;
+  double callSeconds;   /* summed over the backprojection calls (the runner's Total) */
+  double finishSeconds;
+  double totalSeconds;  /* prepare through finish */
+} LolaCudaScanTiming;
+
+int lolaCudaRunScan(RabbitCtGlobalData *data, const float *h_images, size_t imageStride,
+    const double *h_matrices, int count, int callBatch, LolaCudaScanTiming *timing);
+
 /* ---- Autotuning --------------------------------------------------------------
  * No counterpart in the reference (compile-time VECTORSIZE / BLOCKING_FACTOR).
  * Times candidate execution parameters — tile shape (voxels per thread x rows

@@ -97,6 +97,13 @@ class LolaCudaFileReport(C.Structure):
                 ("projections", C.c_int64), ("gups", C.c_double), ("hus", C.c_float * 2)]
 
 
+class LolaCudaScanTiming(C.Structure):
+    _fields_ = [("prepareSeconds", C.c_double),
+                ("callSeconds", C.c_double),
+                ("finishSeconds", C.c_double),
+                ("totalSeconds", C.c_double)]
+
+
 class LolaCudaStats(C.Structure):
     _fields_ = [("passes", C.c_int64),
                 ("packs", C.c_int64),
@@ -172,6 +179,8 @@ _SIGNATURES = [
     ("lolaCudaAutotune", C.c_int, [C.POINTER(LolaCudaGeometry), _P, C.c_size_t, _P, C.c_int,
                                    C.POINTER(LolaCudaConfig), C.POINTER(LolaCudaTuneReport)]),
     ("lolaCudaReadRctHeader", C.c_int, [C.c_char_p, _P, _P, _P, _P]),
+    ("lolaCudaRunScan", C.c_int, [C.POINTER(RabbitCtGlobalData), _P, C.c_size_t, _P, C.c_int,
+                                  C.c_int, C.POINTER(LolaCudaScanTiming)]),
     ("lolaCudaReconstructFile", C.c_int, [C.c_char_p, C.c_int, C.c_float, C.c_float,
                                           C.POINTER(LolaCudaConfig), _P,
                                           C.POINTER(LolaCudaFileReport)]),

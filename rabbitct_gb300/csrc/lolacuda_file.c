@@ -1,4 +1,5 @@
-/* Reconstruction straight from a RabbitCT .rct file (C99).
+/* Reconstruction straight from a RabbitCT .rct file, and the runner's module
+ * loop over projections already in host memory (C99).
  *
  * File format (reference src/ctFileReader_types.h:11-15, src/ctFileReader.c:
  * 47-61): a 20-byte header {u32 width, u32 height, u32 count, f32 hus[2]},
@@ -162,6 +163,51 @@ done:
                    1e9;
     report->hus[0] = hus[0];
     report->hus[1] = hus[1];
+  }
+  return ok;
+}
+
+int lolaCudaRunScan(RabbitCtGlobalData *data, const float *h_images, size_t imageStride,
+    const double *h_matrices, int count, int callBatch, LolaCudaScanTiming *timing)
+{
+  if (data == NULL || (count > 0 && (h_images == NULL || h_matrices == NULL)))
+    return lolaSetError("run scan: null argument");
+  if (count < 0 || callBatch < 1)
+    return lolaSetError("run scan: count %d, call batch %d", count, callBatch);
+  Projection *projs = (Projection *)malloc((size_t)callBatch * sizeof(Projection));
+  if (projs == NULL)
+    return lolaSetError("out of host memory");
+  Projection *savedBuffer = data->projectionBuffer;
+  const uint32_t savedCount = data->numberOfProjections;
+  double calls = 0.0;
+  const double t0 = nowSeconds();
+  int ok = lolaCudaPrepare(data);
+  const double t1 = nowSeconds();
+  for (int done = 0; ok && done < count;) {
+    const int n = (count - done < callBatch) ? count - done : callBatch;
+    for (int i = 0; i < n; ++i) {
+      projs[i].id = done + i + 1;
+      projs[i].matrix = (double *)(h_matrices + 12 * (size_t)(done + i));
+      projs[i].image = (float *)(h_images + imageStride * (size_t)(done + i));
+    }
+    data->projectionBuffer = projs;
+    data->numberOfProjections = (uint32_t)n;
+    const double c0 = nowSeconds();
+    ok = lolaCudaBackprojection(data);
+    calls += nowSeconds() - c0;
+    done += n;
+  }
+  const double t2 = nowSeconds();
+  ok = lolaCudaFinish(data) && ok;
+  const double t3 = nowSeconds();
+  data->projectionBuffer = savedBuffer;
+  data->numberOfProjections = savedCount;
+  free(projs);
+  if (ok && timing != NULL) {
+    timing->prepareSeconds = t1 - t0;
+    timing->callSeconds = calls;
+    timing->finishSeconds = t3 - t2;
+    timing->totalSeconds = t3 - t0;
   }
   return ok;
 }

@@ -355,3 +355,29 @@ def test_runner_output_writers_match_reference_files(lib, tmp_path):
     hist = np.frombuffer(got[off + 16:off + 60], np.uint32)
     assert mse == want["mse_hu2"] and mx == want["max_abs_hu"]    # integer sums: exact
     assert hist.tolist() == want["histogram"] == q["histogram"]
+
+
+@pytest.mark.parametrize("with_geometry", [True, False])
+def test_run_scan_matches_module_loop(lib, scan12, with_geometry):
+    """lolaCudaRunScan (the runner's loop in C) gives exactly the volume of the
+    same module calls made one by one, and reports its phase times."""
+    import ctypes as C
+
+    from rabbitct_gb300._native import LolaCudaScanTiming, check, config
+    from rabbitct_gb300.lolacuda import GlobalData, module_functions
+    from rabbitct_gb300.runner import run_module
+    n = 40
+    vs, o = _geom(n)
+    assert lib.lolaCudaSetConfig(config(batch=5, exit_on_error=0))
+    want = run_module(module_functions(lib, "lolaCuda"), n, vs, o, scan12.matrices,
+                      scan12.images, batch=3, with_geometry=with_geometry).volume
+    imgs = np.ascontiguousarray(scan12.images, np.float32)
+    mats = np.ascontiguousarray(scan12.matrices, np.float64)
+    vol = np.zeros((n, n, n), np.float32)
+    gd = GlobalData(n, vs, o, scan12.width, scan12.height, 1, volume=vol,
+                    geometry=mats if with_geometry else None)
+    t = LolaCudaScanTiming()
+    check(lib.lolaCudaRunScan(gd.ref, imgs.ctypes.data, scan12.width * scan12.height,
+                              mats.ctypes.data, mats.shape[0], 3, C.byref(t)), "run scan")
+    assert np.array_equal(vol, want)
+    assert 0 < t.callSeconds <= t.totalSeconds and t.prepareSeconds > 0
