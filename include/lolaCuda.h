@@ -125,7 +125,14 @@ typedef struct {
                             (N, detector) class at create and use the fastest for
                             its jobs (1), or use voxelsPerThread x rowsPerBlock (0,
                             the default) */
-  int32_t reserved[3];
+  int32_t edgeBatch;     /* projections in the edge passes of a scan, 0 = twice batch,
+                            at most LOLA_MAX_BATCH; batch..LOLA_MAX_BATCH otherwise.
+                            The first pass after an asynchronous volume upload and,
+                            where the module API knows the scan length (-a), its
+                            last pass take this many: the volume transfers they
+                            overlap (one z-chunk at a time) then hide behind more
+                            compute.  Set it to batch for uniform passes. */
+  int32_t reserved[2];
 } LolaCudaConfig;
 
 enum {
@@ -136,11 +143,11 @@ enum {
 /* Defaults: FP32 quad storage (LOLA_STORE_F32Q: the same results as LOLA_STORE_F32,
  * faster), plain accumulation, batch 16, 16 voxels per thread,
  * 4 rows per block, syncEachCall 1, exitOnError 1, no stats, device 0,
- * staging 0.
+ * staging 0, edge passes of twice batch (32).
  * Environment overrides read by lolaCudaDefaultConfig: LOLACUDA_STORAGE
  * (f32|f16|bf16|f32q|f16q|bf16q|tex32|tex16|f16qx|f32qx), LOLACUDA_ACCUM (plain|kahan),
  * LOLACUDA_BATCH, LOLACUDA_VPT, LOLACUDA_ROWS, LOLACUDA_SYNC, LOLACUDA_EXIT,
- * LOLACUDA_STAGING. */
+ * LOLACUDA_STAGING, LOLACUDA_EDGE_BATCH. */
 void lolaCudaDefaultConfig(LolaCudaConfig *config);
 
 /* Configuration used by the next lolaCudaPrepare (module API). */
@@ -202,7 +209,8 @@ int lolaCudaPlanDownloadVolume(LolaCudaPlan *plan, float *h_volume);
 /* Starts the upload of h_volume in z-chunks on the plan's transfer stream and
  * returns; the next pass starts on each chunk as soon as it has landed.
  * h_volume must stay unchanged until lolaCudaPlanSynchronize (page-locked
- * memory makes the call return at once). */
+ * memory makes the call return at once).  The next host-staged pass takes up
+ * to the edge batch of projections (LolaCudaConfig.edgeBatch). */
 int lolaCudaPlanUploadVolumeAsync(LolaCudaPlan *plan, const float *h_volume);
 /* Asks for the volume in h_volume after the next pass: that pass runs in
  * z-chunks and each chunk is copied out as soon as it is finished, so the
@@ -220,7 +228,11 @@ int lolaCudaPlanBackprojectDevice(LolaCudaPlan *plan, const float *d_images,
     size_t imageStride, const double *h_matrices, int count);
 
 /* Same from host images (h_images[p * imageStride + ...]); the images are
- * copied to the device before the call returns. */
+ * copied to the device before the call returns.  Each call closes its last
+ * pass.  Passes take `batch` projections, except the edge passes: the first
+ * after lolaCudaPlanUploadVolumeAsync and, in a call made after
+ * lolaCudaPlanStreamVolumeOut, the last (the pass before it is shortened so
+ * that it is full), which take up to the edge batch. */
 int lolaCudaPlanBackprojectHost(LolaCudaPlan *plan, const float *h_images,
     size_t imageStride, const double *h_matrices, int count);
 

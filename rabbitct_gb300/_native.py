@@ -52,7 +52,8 @@ class LolaCudaConfig(C.Structure):
                 ("batchMode", C.c_int32),
                 ("batchBranches", C.c_int32),
                 ("batchTune", C.c_int32),
-                ("reserved", C.c_int32 * 3)]
+                ("edgeBatch", C.c_int32),
+                ("reserved", C.c_int32 * 2)]
 
 
 class LolaCudaGeometry(C.Structure):
@@ -254,7 +255,8 @@ def config(storage: str | None = None, accumulation: str | None = None,
            rows_per_block: int | None = None, sync_each_call: int | None = None,
            exit_on_error: int = 0, collect_stats: int | None = None, device: int | None = None,
            staging: int | None = None, batch_mode: int | None = None,
-           batch_branches: int | None = None, batch_tune: int | None = None) -> LolaCudaConfig:
+           batch_branches: int | None = None, batch_tune: int | None = None,
+           edge_batch: int | None = None) -> LolaCudaConfig:
     """A LolaCudaConfig from the library's defaults (which honour the
     LOLACUDA_* environment overrides) with the given fields replaced.
     exit_on_error defaults to 0 here: Python callers want exceptions."""
@@ -268,7 +270,8 @@ def config(storage: str | None = None, accumulation: str | None = None,
                         ("rowsPerBlock", rows_per_block), ("syncEachCall", sync_each_call),
                         ("exitOnError", exit_on_error), ("collectStats", collect_stats),
                         ("device", device), ("staging", staging), ("batchMode", batch_mode),
-                        ("batchBranches", batch_branches), ("batchTune", batch_tune)):
+                        ("batchBranches", batch_branches), ("batchTune", batch_tune),
+                        ("edgeBatch", edge_batch)):
         if value is not None:
             setattr(c, name, value)
     return c

@@ -54,7 +54,13 @@ enum { MODE_SKIP = 0, MODE_FAST = 1, MODE_SLOW = 2 };
 #endif
 
 /* Per (tile, projection) setup kept in shared memory for the whole pass. */
-struct TileProj {
+/* 16-byte aligned so that a thread can read its fields from shared memory
+   four at a time (FP32 quads 1298 vs 1261 GUPS at N=1024 on GB300; storing
+   the paired path's constant pairs here as well measured 2-3 % slower) */
+#ifndef LOLA_TILEPROJ_ALIGN
+#define LOLA_TILEPROJ_ALIGN 16
+#endif
+struct __align__(LOLA_TILEPROJ_ALIGN) TileProj {
   float u0, v0, w0;   /* re-centred homogeneous coordinates at the tile origin */
   float cu, cv;       /* pixel offsets: ix = cu + u'/w, iy = cv + v'/w */
   float su[3], sv[3], sw[3]; /* per-axis steps (x, y, z) of u', v', w */

@@ -90,7 +90,9 @@ int lolaCudaReconstructFile(const char *path, int problemSize, float voxelSize, 
   if (!lolaCudaPlanCreate(&g, &c, &plan))
     return 0;
 
-  const int chunk = c.batch;
+  /* chunks are the plan's passes: the edge batch first and last (they
+     overlap the volume transfers), the batch in between */
+  const int chunk = lolaPlanRingSlots(plan);
   const size_t img = (size_t)W * H;
   float *pinned[2] = { NULL, NULL };
   double *mats = (double *)malloc((size_t)2 * chunk * 12 * sizeof(double));
@@ -117,7 +119,10 @@ int lolaCudaReconstructFile(const char *path, int problemSize, float voxelSize, 
     goto done;
   }
   for (uint32_t consumed = 0, k = 0; consumed < count; ++k) {
-    const int n = (count - consumed < (uint32_t)chunk) ? (int)(count - consumed) : chunk;
+    const uint32_t left = count - consumed;
+    int n = lolaPlanPassCapacity(plan, left > (uint32_t)INT32_MAX ? 0 : (int)left);
+    if ((uint32_t)n > left)
+      n = (int)left;
     float *buf = pinned[k & 1];
     double *m = mats + (size_t)(k & 1) * chunk * 12;
     const double r0 = nowSeconds();

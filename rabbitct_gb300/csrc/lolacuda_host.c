@@ -135,6 +135,7 @@ void lolaCudaDefaultConfig(LolaCudaConfig *c)
   /* per-class shape tuning measured no better than the default 16 x 4 tiles on
      the 64-job uneven workload (912 vs 921 GUPS), so it is opt-in */
   c->batchTune = envInt("LOLACUDA_BATCH_TUNE", 0);
+  c->edgeBatch = envInt("LOLACUDA_EDGE_BATCH", 0);
 }
 
 static int validateConfig(const LolaCudaConfig *c)
@@ -145,6 +146,9 @@ static int validateConfig(const LolaCudaConfig *c)
     return setError("invalid accumulation %d", c->accumulation);
   if (c->batch < 1 || c->batch > LOLA_MAX_BATCH)
     return setError("batch %d outside 1..%d", c->batch, LOLA_MAX_BATCH);
+  if (c->edgeBatch != 0 && (c->edgeBatch < c->batch || c->edgeBatch > LOLA_MAX_BATCH))
+    return setError("edge batch %d outside %d..%d (or 0)", c->edgeBatch, c->batch,
+        LOLA_MAX_BATCH);
   if (!lolaKernelShapeSupported(c->voxelsPerThread, c->rowsPerBlock))
     return setError("no kernel for %d voxels per thread x %d rows per block",
         c->voxelsPerThread, c->rowsPerBlock);
@@ -213,6 +217,10 @@ struct LolaCudaPlan {
   float *outValid;   /* host copy streamed out after the last pass, if any */
   /* host-staged batch (module API / BackprojectHost) */
   int pending;
+  int passCap;    /* projections the pass being staged takes before it launches */
+  int ringSlots;  /* stage and ring slots: the larger of batch and the edge batch */
+  int scanLeft;   /* projections of the scan not yet staged, this one included
+                     (0 = unknown); set by the module API before each stage */
   double pendingMats[LOLA_MAX_BATCH][12];
   /* statistics */
   LolaCudaStats stats;
@@ -349,14 +357,18 @@ static int planInit(LolaCudaPlan *p)
   s->slotElems = (px + 255) & ~(size_t)255;  /* slot bases 512 B aligned */
   p->imageElems = (size_t)g->imageWidth * (size_t)g->imageHeight;
 
+  p->ringSlots = p->cfg.edgeBatch > p->cfg.batch ? p->cfg.edgeBatch
+      : p->cfg.edgeBatch == 0 ? 2 * p->cfg.batch : p->cfg.batch;
+  if (p->ringSlots > LOLA_MAX_BATCH)
+    p->ringSlots = LOLA_MAX_BATCH;
   const size_t nvox = lolaPlanVoxels(p);
   CUDA_TRY(cudaMalloc((void **)&p->d_volume, nvox * sizeof(float)));
   CUDA_TRY(cudaMemsetAsync(p->d_volume, 0, nvox * sizeof(float), p->stream));
-  CUDA_TRY(cudaMalloc(&p->d_ring, (size_t)p->cfg.batch * s->slotElems * s->elemBytes));
-  CUDA_TRY(cudaMemsetAsync(p->d_ring, 0, (size_t)p->cfg.batch * s->slotElems * s->elemBytes,
+  CUDA_TRY(cudaMalloc(&p->d_ring, (size_t)p->ringSlots * s->slotElems * s->elemBytes));
+  CUDA_TRY(cudaMemsetAsync(p->d_ring, 0, (size_t)p->ringSlots * s->slotElems * s->elemBytes,
       p->stream));
   if (isTexture(s->storage)) {
-    for (int i = 0; i < p->cfg.batch; i++) {
+    for (int i = 0; i < p->ringSlots; i++) {
       struct cudaResourceDesc rd;
       memset(&rd, 0, sizeof(rd));
       rd.resType = cudaResourceTypePitch2D;
@@ -392,7 +404,8 @@ static int planInit(LolaCudaPlan *p)
       s->texObjects[i] = (unsigned long long)t;
     }
   }
-  CUDA_TRY(cudaMalloc((void **)&p->d_stage, (size_t)p->cfg.batch * p->imageElems * sizeof(float)));
+  CUDA_TRY(cudaMalloc((void **)&p->d_stage,
+      (size_t)p->ringSlots * p->imageElems * sizeof(float)));
   CUDA_TRY(cudaMalloc((void **)&p->d_counters, LOLA_TILE_COUNTERS * sizeof(unsigned long long)));
   CUDA_TRY(cudaMemsetAsync(p->d_counters, 0, LOLA_TILE_COUNTERS * sizeof(unsigned long long),
       p->stream));
@@ -762,7 +775,7 @@ static int prepareStage(LolaCudaPlan *p, const double *mats, int count)
   if (bw != p->stageBoxW || bh != p->stageBoxH) {
     const LolaStoreDesc *st = &p->store;
     cuuint64_t dims[3] = { (cuuint64_t)st->pitch * epp, (cuuint64_t)st->rows,
-      (cuuint64_t)p->cfg.batch };
+      (cuuint64_t)p->ringSlots };
     cuuint64_t strides[2] = { (cuuint64_t)st->pitch * pix, (cuuint64_t)st->slotElems * pix };
     cuuint32_t box[3] = { (cuuint32_t)(bw * epp), (cuuint32_t)bh, 1 };
     cuuint32_t estr[3] = { 1, 1, 1 };
@@ -926,16 +939,47 @@ static int flushPending(LolaCudaPlan *p)
   return launchPass(p, &p->pendingMats[0][0], n);
 }
 
-/* Stages one host projection; flushes when the ring is full. */
+/* Projections the next host-staged pass takes.  Edge passes take the edge
+ * batch: the first pass after an asynchronous upload (it starts on each
+ * z-chunk as the chunk lands, so more projections per chunk hide more of the
+ * upload) and the last pass of a scan of known length (it streams each chunk
+ * out as it finishes, likewise).  The pass before the last one is shortened
+ * where needed so that the last one is full.  With the edge batch equal to
+ * the batch every pass takes the batch, the last one what is left. */
+static int passCapacity(const LolaCudaPlan *p, int left)
+{
+  int cap = p->uploadChunks > 0 ? p->ringSlots : p->cfg.batch;
+  if (left > 0 && p->ringSlots > p->cfg.batch) {
+    if (left <= p->ringSlots)
+      cap = left;
+    else if (cap > left - p->ringSlots)
+      cap = left - p->ringSlots;
+  }
+  return cap;
+}
+
+int lolaPlanPassCapacity(const LolaCudaPlan *p, int left)
+{
+  return passCapacity(p, left);
+}
+
+int lolaPlanRingSlots(const LolaCudaPlan *p)
+{
+  return p->ringSlots;
+}
+
+/* Stages one host projection; flushes when the pass is complete. */
 static int stageHost(LolaCudaPlan *p, const float *image, const double *matrix, int *flushed)
 {
-  if (p->pending == 0)
+  if (p->pending == 0) {
     CUDA_TRY(cudaStreamWaitEvent(p->copyStream, p->stageFree, 0));
+    p->passCap = passCapacity(p, p->scanLeft);
+  }
   CUDA_TRY(cudaMemcpyAsync(p->d_stage + (size_t)p->pending * p->imageElems, image,
       p->imageElems * sizeof(float), cudaMemcpyHostToDevice, p->copyStream));
   memcpy(p->pendingMats[p->pending], matrix, 12 * sizeof(double));
   p->pending++;
-  if (p->pending == p->cfg.batch) {
+  if (p->pending >= p->passCap) {
     if (!flushPending(p))
       return 0;
     *flushed = 1;
@@ -954,9 +998,17 @@ int lolaCudaPlanBackprojectHost(LolaCudaPlan *p, const float *h_images, size_t i
     return setError("null argument");
   CUDA_TRY(cudaSetDevice(p->device));
   int flushed = 0;
-  for (int i = 0; i < count; i++)
-    if (!stageHost(p, h_images + (size_t)i * imageStride, h_mats + 12 * (size_t)i, &flushed))
+  /* a call whose last pass streams the volume out is the end of its scan:
+     that pass takes the edge batch */
+  const int tail = p->streamOut != NULL;
+  for (int i = 0; i < count; i++) {
+    p->scanLeft = tail ? count - i : 0;
+    if (!stageHost(p, h_images + (size_t)i * imageStride, h_mats + 12 * (size_t)i, &flushed)) {
+      p->scanLeft = 0;
       return 0;
+    }
+  }
+  p->scanLeft = 0;
   if (!flushPending(p))
     return 0;
   CUDA_TRY(cudaStreamSynchronize(p->copyStream));
@@ -1235,6 +1287,8 @@ int lolaCudaBackprojection(RabbitCtGlobalData *d)
       return moduleFail("backprojection");
     }
     const int last = gTotalProjections > 0 && pr->id >= (int)gTotalProjections;
+    p->scanLeft = gTotalProjections > 0 && pr->id >= 1 && pr->id <= (int)gTotalProjections
+        ? (int)gTotalProjections - pr->id + 1 : 0;
     /* the scan's last pass copies the volume out chunk by chunk as it
        finishes them, overlapping the download with the pass's tail; only
        into page-locked memory, where the copies do not hold up this (timed)

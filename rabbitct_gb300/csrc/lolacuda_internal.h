@@ -153,6 +153,10 @@ int lolaLaunchBackproject(const LolaStoreDesc *store, const LolaPassParams *para
 /* Voxels of a plan's volume (N^3). */
 size_t lolaPlanVoxels(const LolaCudaPlan *plan);
 const LolaCudaGeometry *lolaPlanGeometry(const LolaCudaPlan *p);
+/* Projections the plan's next host-staged pass takes with `left` projections
+   of the scan still to stage (0 = unknown), and the most any pass takes. */
+int lolaPlanPassCapacity(const LolaCudaPlan *p, int left);
+int lolaPlanRingSlots(const LolaCudaPlan *p);
 
 /* Sets the thread's lolaCudaLastError() message; returns 0. */
 int lolaSetError(const char *fmt, ...);

@@ -38,12 +38,16 @@ def _initial(depth, n, seed=5):
     return (rng.standard_normal((depth, n, n)) * 1e-3).astype(np.float32)
 
 
-def _sync_result(scan, n, init, slab, **kw):
+def _sync_result(scan, n, init, slab, splits=(), **kw):
+    """The synchronous path; `splits` are the projection indices where a new
+    pass starts beyond those the batch makes (each host call closes a pass)."""
     from rabbitct_gb300.lolacuda import Plan
     vs, o = _geom(n)
+    cuts = [0, *splits, scan.images.shape[0]]
     with Plan(n, vs, o, scan.width, scan.height, slab=slab, **kw) as p:
         p.upload(init)
-        p.backproject_host(scan.images, scan.matrices)
+        for a, b in zip(cuts[:-1], cuts[1:]):
+            p.backproject_host(scan.images[a:b], scan.matrices[a:b])
         return p.download()
 
 
@@ -87,6 +91,32 @@ def test_single_pass_overlaps_both_transfers(lib, scan7):
     assert st.overlappedPasses == 1
 
 
+def test_first_pass_after_upload_takes_the_edge_batch(lib, scan7):
+    """After an asynchronous upload the first host-staged pass takes the edge
+    batch (4 here), the rest the batch (2): passes of 4, 2 and 1."""
+    from rabbitct_gb300.lolacuda import Plan
+    init = _initial(N, N, seed=9)
+    want = _sync_result(scan7, N, init, None, splits=(4, 6), batch=4)
+    vs, o = _geom(N)
+    with Plan(N, vs, o, scan7.width, scan7.height, batch=2, edge_batch=4,
+              collect_stats=1) as p:
+        p.upload_async(init.copy())
+        p.backproject_host(scan7.images, scan7.matrices)
+        out = p.download()
+        st = p.stats()
+    assert st.passes == 3 and st.overlappedPasses == 1
+    assert np.array_equal(out, want)
+
+
+def test_edge_batch_is_validated(lib):
+    from rabbitct_gb300._native import LolaCudaError
+    from rabbitct_gb300.lolacuda import Plan
+    vs, o = _geom(16)
+    for edge in (3, 33):
+        with pytest.raises(LolaCudaError, match="edge batch"):
+            Plan(16, vs, o, 64, 48, batch=4, edge_batch=edge)
+
+
 def test_transfers_order_against_other_volume_work(lib, scan7):
     """An asynchronous upload followed by a zeroing, and a stream-out request
     with no pass before synchronize (a plain copy of the volume)."""
@@ -105,19 +135,25 @@ def test_transfers_order_against_other_volume_work(lib, scan7):
     assert np.array_equal(again, want)
 
 
+@pytest.mark.parametrize("edge", [0, 3])
 @pytest.mark.parametrize("pinned", [True, False])
 @pytest.mark.parametrize("with_geometry", [True, False])
-def test_module_api_overlap_matches_plan(lib, scan7, with_geometry, pinned):
+def test_module_api_overlap_matches_plan(lib, scan7, with_geometry, pinned, edge):
     """prepare uploads asynchronously; into a page-locked volume the scan's
     last call (with -a) or finish's closing pass (without) streams the volume
-    out, a pageable one is copied in finish."""
+    out, a pageable one is copied in finish.
+
+    Passes of 7 projections at batch 3: with the default edge batch (6) the
+    first pass takes 6 where the scan length is unknown (6 + 1) and the last
+    pass takes 6 where it is known (1 + 6); with edge batch 3, 3 + 3 + 1."""
     import ctypes as C
 
     from rabbitct_gb300._native import config
     from rabbitct_gb300.lolacuda import module_functions
     from rabbitct_gb300.runner import run_module
     init = _initial(N, N, seed=8)
-    want = _sync_result(scan7, N, init, None, batch=3)
+    splits = (3, 6) if edge == 3 else (1,) if with_geometry else (6,)
+    want = _sync_result(scan7, N, init, None, splits=splits, batch=6)
     vs, o = _geom(N)
     host = None
     if pinned:
@@ -129,7 +165,8 @@ def test_module_api_overlap_matches_plan(lib, scan7, with_geometry, pinned):
     else:
         vol = init.copy()
     try:
-        assert lib.lolaCudaSetConfig(config(storage="f32", batch=3, exit_on_error=0))
+        assert lib.lolaCudaSetConfig(config(storage="f32", batch=3, edge_batch=edge,
+                                            exit_on_error=0))
         r = run_module(module_functions(lib, "lolaCuda"), N, vs, o, scan7.matrices,
                        scan7.images, batch=1, with_geometry=with_geometry, volume=vol)
         assert np.array_equal(r.volume, want)

@@ -298,8 +298,12 @@ def test_reconstruct_from_rct_file(lib, tmp_path, batch):
     vs, o = _geom(n)
     vol, rep = reconstruct_file(path, n, vs, o, batch=batch)
     assert rep["projections"] == 11 and rep["hus"] == pytest.approx(scan.hus)
-    with Plan(n, vs, o, scan.width, scan.height, batch=batch) as plan:
-        plan.backproject_host(scan.images, scan.matrices)
+    # the file is read in the plan's passes: edge batch (2 x batch) first and
+    # last, the last one full: 5 + 6 at batch 3, all 11 at once at batch 16
+    cuts = [0, 5, 11] if batch == 3 else [0, 11]
+    with Plan(n, vs, o, scan.width, scan.height, batch=min(32, 2 * batch)) as plan:
+        for a, b in zip(cuts[:-1], cuts[1:]):
+            plan.backproject_host(scan.images[a:b], scan.matrices[a:b])
         want = plan.download()
     assert np.array_equal(vol, want)
     ref = oracle.bunny_f64(n, vs, o, scan.matrices, scan.images)
