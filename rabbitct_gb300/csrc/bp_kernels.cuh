@@ -53,6 +53,12 @@ enum { MODE_SKIP = 0, MODE_FAST = 1, MODE_SLOW = 2 };
 #define LOLA_PAIRED 1
 #endif
 
+/* 1: the per-tile setup reads the pass's projections from their device copy
+   (LolaPassParams.projDevice) where the host provides one */
+#ifndef LOLA_PROJ_DEVICE
+#define LOLA_PROJ_DEVICE 1
+#endif
+
 /* Per (tile, projection) setup kept in shared memory for the whole pass. */
 /* 16-byte aligned so that a thread can read its fields from shared memory
    four at a time (FP32 quads 1298 vs 1261 GUPS at N=1024 on GB300; storing
@@ -726,7 +732,12 @@ __device__ __forceinline__ void setupTile(const LolaPassParams &P, const PassArg
   g.width = a.width;
   g.height = a.height;
   g.margin = a.margin;
-  setupTileGeom<ROWS, VPT, TX>(P.proj, P.count, g, sp, tid, nthreads, x0, y0, z0);
+#if LOLA_PROJ_DEVICE
+  const LolaPassProj *proj = P.projDevice != nullptr ? P.projDevice : P.proj;
+#else
+  const LolaPassProj *proj = P.proj;
+#endif
+  setupTileGeom<ROWS, VPT, TX>(proj, P.count, g, sp, tid, nthreads, x0, y0, z0);
 }
 
 /* Resident blocks per SM requested from the register allocator.  The pass is

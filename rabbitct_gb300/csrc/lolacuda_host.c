@@ -200,6 +200,7 @@ struct LolaCudaPlan {
   cudaArray_t texArrays[LOLA_MAX_BATCH];  /* texture layouts with LOLA_TEX_ARRAYS */
   float *d_stage;
   unsigned long long *d_counters;
+  LolaPassProj *d_proj;   /* device copy of the current pass's projections */
   int *d_error;           /* staged-pass wait timeouts */
   int stagedLaunched;     /* a staged pass ran since the last error check */
   LolaStageDesc stageDesc; /* tensor map of the ring for the current box */
@@ -287,6 +288,7 @@ static int planRelease(LolaCudaPlan *p)
   cudaFree(p->d_ring);
   cudaFree(p->d_stage);
   cudaFree(p->d_counters);
+  cudaFree(p->d_proj);
   cudaFree(p->d_error);
   if (p->stageFree)
     cudaEventDestroy(p->stageFree);
@@ -407,6 +409,7 @@ static int planInit(LolaCudaPlan *p)
   CUDA_TRY(cudaMalloc((void **)&p->d_stage,
       (size_t)p->ringSlots * p->imageElems * sizeof(float)));
   CUDA_TRY(cudaMalloc((void **)&p->d_counters, LOLA_TILE_COUNTERS * sizeof(unsigned long long)));
+  CUDA_TRY(cudaMalloc((void **)&p->d_proj, LOLA_MAX_BATCH * sizeof(LolaPassProj)));
   CUDA_TRY(cudaMemsetAsync(p->d_counters, 0, LOLA_TILE_COUNTERS * sizeof(unsigned long long),
       p->stream));
   CUDA_TRY(cudaMalloc((void **)&p->d_error, sizeof(int)));
@@ -830,6 +833,10 @@ static int launchPass(LolaCudaPlan *p, const double *mats, int count)
   P.countTiles = p->cfg.collectStats;
   for (int i = 0; i < count; i++)
     fillPassProj(&P.proj[i], mats + 12 * (size_t)i, p->geom.voxelSize, i);
+  /* stream-ordered: the copy lands after the previous pass has read it */
+  CUDA_TRY(cudaMemcpyAsync(p->d_proj, P.proj, (size_t)count * sizeof(LolaPassProj),
+      cudaMemcpyHostToDevice, p->stream));
+  P.projDevice = p->d_proj;
   EventPair *ev = NULL;
   if (p->cfg.collectStats) {
     if (!pushEvent(p, &ev))

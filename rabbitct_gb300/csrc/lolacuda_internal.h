@@ -69,6 +69,11 @@ typedef struct {
   int32_t voxelsPerThread;
   int32_t rowsPerBlock;
   int32_t countTiles;   /* accumulate fast/slow/skipped tile counters */
+  /* device copy of proj[0 .. count), or null.  The per-tile setup reads each
+     projection from one lane; from the kernel parameters those reads differ
+     per lane and the constant cache serves them one address at a time, from
+     global memory they are ordinary cached loads */
+  const LolaPassProj *projDevice;
   LolaPassProj proj[LOLA_MAX_BATCH];
 } LolaPassParams;
 

@@ -155,6 +155,7 @@ extern "C" int lolaCudaBackprojectNoAlloc(const LolaCudaGeometry *g, const LolaC
     P.voxelsPerThread = c.voxelsPerThread;
     P.rowsPerBlock = c.rowsPerBlock;
     P.countTiles = 0;
+    P.projDevice = nullptr;  /* projections from the kernel parameters */
     for (int i = 0; i < n; i++) {
       const double *m = h_matrices + 12 * (size_t)(done + i);
       LolaPassProj &pp = P.proj[i];
