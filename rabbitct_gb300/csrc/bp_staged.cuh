@@ -144,7 +144,8 @@ template <> struct SharedTaps<LOLA_STORE_BF16> {
   }
 };
 
-template <> struct SharedTaps<LOLA_STORE_F32Q> {
+/* FP32 quads in the order Layout<S> stores them */
+template <bool COLS> struct SharedQuadF32 {
   static constexpr bool kQuad = true;
   static constexpr bool kDiff = false;
   __device__ static __forceinline__ void fetch(const unsigned char *b, uint32_t i, int,
@@ -152,11 +153,14 @@ template <> struct SharedTaps<LOLA_STORE_F32Q> {
   {
     const float4 q = reinterpret_cast<const float4 *>(b)[i];
     p00 = q.x;
-    p10 = q.y;
-    p01 = q.z;
+    p10 = COLS ? q.z : q.y;
+    p01 = COLS ? q.y : q.z;
     p11 = q.w;
   }
 };
+
+template <> struct SharedTaps<LOLA_STORE_F32Q>
+    : SharedQuadF32<Layout<LOLA_STORE_F32Q>::kCols> {};
 
 template <> struct SharedTaps<LOLA_STORE_F16Q> {
   static constexpr bool kQuad = true;
@@ -189,7 +193,8 @@ template <> struct SharedTaps<LOLA_STORE_BF16Q> {
 };
 
 template <> struct SharedTaps<LOLA_STORE_F16QX> : SharedTaps<LOLA_STORE_F16Q> {};
-template <> struct SharedTaps<LOLA_STORE_F32QX> : SharedTaps<LOLA_STORE_F32Q> {};
+template <> struct SharedTaps<LOLA_STORE_F32QX>
+    : SharedQuadF32<Layout<LOLA_STORE_F32QX>::kCols> {};
 
 /* Applies one staged projection to the thread's VPT voxels (unclamped: only
  * tiles on the fast path are staged). */
@@ -254,8 +259,8 @@ __device__ __forceinline__ void applyStagedPairs(const TileProj &tp, const unsig
   /* 2^23 + box-local index of pixel (cu, cv), which lies in the box (the tile
      origin's own pixel is inside its footprint) */
   const float kxc = fmaf(tp.cv + tp.syo, (float)g.boxW, tp.sxm + tp.cu);
-  pairedUpdate<VPT, KAHAN, SharedTaps<S>::kDiff>(tp, fi, fj, kxc, (float)g.boxW, fetch, acc,
-      comp);
+  pairedUpdate<VPT, KAHAN, SharedTaps<S>::kDiff, false>(tp, fi, fj, kxc, (float)g.boxW, fetch,
+      acc, comp);
 }
 
 #ifndef LOLA_STAGED_MIN_BLOCKS

@@ -160,6 +160,32 @@ def test_fast_path_exercised(lib):
     assert st.tilePassesFast > 0
 
 
+@pytest.mark.parametrize("storage", ["f32q", "f32qx"])
+def test_fp32_quads_equal_plain_fp32(lib, storage):
+    """FP32 quads hold the exact FP32 taps (f32q column by column, read by one
+    16-byte load; f32qx row by row, by a load or one texel), and the paired
+    path's column-pair interpolation rounds as the plain layout's pairwise
+    one: the volumes are identical.
+    Full-size detector, N=128, 16 x 4 and 8 x 8 tiles: paired, one-voxel and
+    clamped tiles all occur."""
+    from rabbitct_gb300.lolacuda import Plan
+    spec = synth.ScanSpec(nproj=6, seed=3)
+    scan = synth.make_scan(spec)
+    n = 128
+    vs = synth.voxel_size(n)
+    o = synth.origin_index(n, vs)
+    for vpt, rows in ((16, 4), (8, 8)):
+        vols, stats = [], []
+        for st_name in ("f32", storage):
+            with Plan(n, vs, o, spec.width, spec.height, storage=st_name, batch=6,
+                      voxels_per_thread=vpt, rows_per_block=rows, collect_stats=1) as plan:
+                plan.backproject_host(scan.images, scan.matrices)
+                vols.append(plan.download())
+                stats.append(plan.stats())
+        assert stats[1].tilePassesPaired > 0 and stats[1].tilePassesSlow > 0
+        assert np.array_equal(vols[1], vols[0]), (vpt, rows)
+
+
 @pytest.mark.parametrize("batch_call", [1, 3])
 @pytest.mark.parametrize("with_geometry", [True, False])
 def test_module_api_like_runner(lib, scan12, batch_call, with_geometry):
