@@ -244,10 +244,13 @@ template <bool COLS> struct QuadF32Layout {
 
 template <> struct Layout<LOLA_STORE_F32Q> : QuadF32Layout<LOLA_F32Q_COLS> {};
 
-template <> struct Layout<LOLA_STORE_F16Q> {
+/* FP16 quads: four halves per pixel, the taps or (LOLA_QUAD_TERMS) the
+ * bilinear terms, in the slots (00, 10, 01, 11), or with COLS in the order
+ * (00, 01, 10, 11).  fetch returns them by slot name. */
+template <bool COLS> struct QuadF16Layout {
   static constexpr bool kTex = false;
   static constexpr bool kMixed = false;
-  static constexpr bool kCols = false;
+  static constexpr bool kCols = COLS;
   typedef uint2 Elem;
   static constexpr bool kQuad = true;
   static constexpr bool kDiff = LOLA_QUAD_TERMS;
@@ -261,22 +264,24 @@ template <> struct Layout<LOLA_STORE_F16Q> {
     const float2 a = __half22float2(lo);
     const float2 b = __half22float2(hi);
     p00 = a.x;
-    p10 = a.y;
-    p01 = b.x;
+    p10 = COLS ? b.x : a.y;
+    p01 = COLS ? a.y : b.x;
     p11 = b.y;
   }
   __device__ static __forceinline__ void store(void *dst, size_t o, float a, float b, float c,
       float d)
   {
     const float4 t = LOLA_QUAD_TERMS ? bilinearTerms(a, b, c, d) : make_float4(a, b, c, d);
-    const __half2 lo = __floats2half2_rn(t.x, t.y);
-    const __half2 hi = __floats2half2_rn(t.z, t.w);
+    const __half2 lo = COLS ? __floats2half2_rn(t.x, t.z) : __floats2half2_rn(t.x, t.y);
+    const __half2 hi = COLS ? __floats2half2_rn(t.y, t.w) : __floats2half2_rn(t.z, t.w);
     uint2 q;
     q.x = *reinterpret_cast<const uint32_t *>(&lo);
     q.y = *reinterpret_cast<const uint32_t *>(&hi);
     static_cast<uint2 *>(dst)[o] = q;
   }
 };
+
+template <> struct Layout<LOLA_STORE_F16Q> : QuadF16Layout<false> {};
 
 template <> struct Layout<LOLA_STORE_BF16Q> {
   static constexpr bool kTex = false;
@@ -356,7 +361,21 @@ __device__ __forceinline__ void texTaps(unsigned long long tex, float cx, float 
  * texture unit (a point fetch, widened to FP32 there), the others through the
  * load path, so both gather pipes work in parallel. */
 
-template <> struct Layout<LOLA_STORE_F16QX> : Layout<LOLA_STORE_F16Q> {
+/* 1: f16qx stores its quads column by column, and its texture-read voxels
+   are paired in the texture mask LOLA_MIXED_COLS_TEX_MASK (both voxels of a
+   pair by texture or both by loads): a texel then lands as the two column
+   pairs that one packed FMA interpolates in x.  Measured on GB300 at N=1024:
+   1471 GUPS vs 1470 for the row order with mask 0xAAAA (and 1419 for the row
+   order with mask 0xCCCC, whose texture pairs need register moves), so the
+   default stays the row order */
+#ifndef LOLA_F16QX_COLS
+#define LOLA_F16QX_COLS 0
+#endif
+#ifndef LOLA_MIXED_COLS_TEX_MASK
+#define LOLA_MIXED_COLS_TEX_MASK 0xCCCCu
+#endif
+
+template <> struct Layout<LOLA_STORE_F16QX> : QuadF16Layout<LOLA_F16QX_COLS> {
   static constexpr bool kMixed = true;
 };
 
@@ -539,10 +558,11 @@ __device__ __forceinline__ void applyProjection(const TileProj &tp, const void *
  * xm + floor(qv) * rowPitch.
  * fetch(k, idxf, nqx, nqy, p00, p10, p01, p11) reads voxel k's taps given
  * idxf = 2^23 + its pixel index, and nqx = cu - floor(ix), nqy = cv - floor(iy)
- * (integers).  COLS: fetch delivers the taps column by column, (p00, p01,
- * p10, p11), and each voxel is interpolated in x with one packed FMA over its
- * two column pairs (the same roundings as the pairwise form below). */
-template <int VPT, bool KAHAN, bool DIFF, bool COLS, class Fetch>
+ * (integers).  Voxel pairs whose bits are both set in COLSMASK get their taps
+ * (or terms) column by column, (00, 01, 10, 11), and each voxel is
+ * interpolated in x with one packed FMA over its two column pairs (the same
+ * roundings as the pairwise form below). */
+template <int VPT, bool KAHAN, bool DIFF, unsigned COLSMASK, class Fetch>
 __device__ __forceinline__ void pairedUpdate(const TileProj &tp, float fi, float fj, float kxc,
     float rowPitch, Fetch fetch, float2 (&acc)[VPT / 2], float2 (&comp)[VPT / 2])
 {
@@ -582,7 +602,7 @@ __device__ __forceinline__ void pairedUpdate(const TileProj &tp, float fi, float
     const float2 AY = __fadd2_rn(QV, TY);
     const float2 IDX = __ffma2_rn(TY, npitch, XM);  /* 2^23 + pixel index */
     float2 VAL;
-    if (COLS && !DIFF) {
+    if (((COLSMASK >> (2 * j)) & 3u) == 3u) {
       float val[2];
 #pragma unroll
       for (int h = 0; h < 2; ++h) {
@@ -590,9 +610,15 @@ __device__ __forceinline__ void pairedUpdate(const TileProj &tp, float fi, float
         fetch(2 * j + h, h ? IDX.y : IDX.x, h ? TX.y : TX.x, h ? TY.y : TY.x, q0, q1, q2, q3);
         const float2 c0 = make_float2(q0, q1), c1 = make_float2(q2, q3);
         const float ax = h ? AX.y : AX.x, ay = h ? AY.y : AY.x;
-        /* (p10 - p00, p11 - p01), then the rows' x interpolants (b, t) */
-        const float2 bt = __ffma2_rn(make_float2(ax, ax), __ffma2_rn(c0, neg1, c1), c0);
-        val[h] = fmaf(ay, fmaf(bt.x, -1.0f, bt.y), bt.x);
+        if (DIFF) {
+          /* terms (t0, t2), (t1, t3): the rows' x interpolants (b, c) */
+          const float2 bc = __ffma2_rn(make_float2(ax, ax), c1, c0);
+          val[h] = fmaf(ay, bc.y, bc.x);
+        } else {
+          /* (p10 - p00, p11 - p01), then the rows' x interpolants (b, t) */
+          const float2 bt = __ffma2_rn(make_float2(ax, ax), __ffma2_rn(c0, neg1, c1), c0);
+          val[h] = fmaf(ay, fmaf(bt.x, -1.0f, bt.y), bt.x);
+        }
       }
       VAL = make_float2(val[0], val[1]);
     } else {
@@ -626,7 +652,16 @@ __device__ __forceinline__ void pairedUpdate(const TileProj &tp, float fi, float
   }
 }
 
-/* The paired update on the stored ring (loads, texture or both). */
+/* Texture mask of a mixed layout in the pass kernel. */
+template <int S> struct PassTexMask {
+  static constexpr unsigned kValue = Layout<S>::kCols ? LOLA_MIXED_COLS_TEX_MASK
+                                                      : LOLA_MIXED_TEX_MASK;
+};
+
+/* The paired update on the stored ring (loads, texture or both).  Voxels
+ * whose fetch delivers column pairs (every voxel of a column-ordered load
+ * layout; the texture voxels of a column-ordered mixed layout) are
+ * interpolated per voxel; the rest pairwise. */
 template <int S, int VPT, bool KAHAN, class A, unsigned TEXMASK = LOLA_MIXED_TEX_MASK>
 __device__ __forceinline__ void applyPairs(const TileProj &tp, const void *img,
     unsigned long long tex, const A &a, float fi, float fj, float2 (&acc)[VPT / 2],
@@ -645,25 +680,35 @@ __device__ __forceinline__ void applyPairs(const TileProj &tp, const void *img,
      halves) */
   const float toff = margin + (Layout<S>::kTex ? 1.0f : 0.5f);
   const float tcx = tp.cu + toff, tcy = tp.cv + toff;
+  /* voxels whose fetch returns the stored components in stored order: all
+     of a column-ordered load layout; of a mixed one, the texture voxels of
+     pairs read wholly through the texture */
+  constexpr unsigned kTexPairs = TEXMASK & (TEXMASK >> 1) & 0x55555555u;
+  constexpr unsigned COLSMASK = !Layout<S>::kCols ? 0u
+                                : Layout<S>::kMixed ? (kTexPairs | (kTexPairs << 1))
+                                                    : 0xffffffffu;
   auto fetch = [&](int k, float idxf, float nqx, float nqy, float &p00, float &p10, float &p01,
                    float &p11) {
     if constexpr (Layout<S>::kTex) {
       texTaps(tex, tcx - nqx, tcy - nqy, p00, p10, p01, p11);
     } else {
       if (Layout<S>::kMixed && ((TEXMASK >> k) & 1u)) {
-        texQuad<Layout<S>::kCols, true>(tex, tcx - nqx, tcy - nqy, p00, p10, p01, p11);
+        if ((COLSMASK >> k) & 1u)
+          texQuad<Layout<S>::kCols, true>(tex, tcx - nqx, tcy - nqy, p00, p10, p01, p11);
+        else
+          texQuad<Layout<S>::kCols>(tex, tcx - nqx, tcy - nqy, p00, p10, p01, p11);
       } else {
         uint32_t idx = __float_as_uint(idxf) - 0x4B000000u;
         idx = min(idx, maxIdx);  /* memory-safety net; never active on valid input */
-        if constexpr (Layout<S>::kCols)
+        if constexpr (Layout<S>::kCols && !Layout<S>::kMixed)
           Layout<S>::fetchRaw(img, idx, pitch, p00, p10, p01, p11);
         else
           Layout<S>::fetch(img, idx, pitch, p00, p10, p01, p11);
       }
     }
   };
-  pairedUpdate<VPT, KAHAN, Layout<S>::kDiff, Layout<S>::kCols>(tp, fi, fj, kxc,
-      (float)a.pitch, fetch, acc, comp);
+  pairedUpdate<VPT, KAHAN, Layout<S>::kDiff, COLSMASK>(tp, fi, fj, kxc, (float)a.pitch, fetch,
+      acc, comp);
 }
 
 /* Per-(tile, projection) setup shared by the pass kernels: the FP64 tile
@@ -899,12 +944,13 @@ __global__ void __launch_bounds__(32 * ROWS, LOLA_PASS_MIN_BLOCKS(S, VPT, ROWS))
     const void *img = static_cast<const char *>(a.ring) + (size_t)tp.slot * a.slotBytes;
     const unsigned long long tex =
         (Layout<S>::kTex || Layout<S>::kMixed) ? a.tex[tp.slot] : 0ull;
+    constexpr unsigned kMask = PassTexMask<S>::kValue;
     if (mode == MODE_FAST && tp.pos && LOLA_PAIRED)
-      applyPairs<S, VPT, KAHAN>(tp, img, tex, a, fi, fj, acc, comp);
+      applyPairs<S, VPT, KAHAN, PassArgs, kMask>(tp, img, tex, a, fi, fj, acc, comp);
     else if (mode == MODE_FAST)
-      applyProjection<S, VPT, KAHAN, false>(tp, img, tex, a, fi, fj, acc, comp);
+      applyProjection<S, VPT, KAHAN, false, PassArgs, kMask>(tp, img, tex, a, fi, fj, acc, comp);
     else
-      applyProjection<S, VPT, KAHAN, true>(tp, img, tex, a, fi, fj, acc, comp);
+      applyProjection<S, VPT, KAHAN, true, PassArgs, kMask>(tp, img, tex, a, fi, fj, acc, comp);
   }
   float *vcol = column();
 #pragma unroll

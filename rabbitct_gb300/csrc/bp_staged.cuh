@@ -162,7 +162,8 @@ template <bool COLS> struct SharedQuadF32 {
 template <> struct SharedTaps<LOLA_STORE_F32Q>
     : SharedQuadF32<Layout<LOLA_STORE_F32Q>::kCols> {};
 
-template <> struct SharedTaps<LOLA_STORE_F16Q> {
+/* FP16 quads in the order Layout<S> stores them */
+template <bool COLS> struct SharedQuadF16 {
   static constexpr bool kQuad = true;
   static constexpr bool kDiff = LOLA_QUAD_TERMS;  /* as stored by Layout<S> */
   __device__ static __forceinline__ void fetch(const unsigned char *b, uint32_t i, int,
@@ -172,11 +173,13 @@ template <> struct SharedTaps<LOLA_STORE_F16Q> {
     const float2 lo = __half22float2(*reinterpret_cast<const __half2 *>(&q.x));
     const float2 hi = __half22float2(*reinterpret_cast<const __half2 *>(&q.y));
     p00 = lo.x;
-    p10 = lo.y;
-    p01 = hi.x;
+    p10 = COLS ? hi.x : lo.y;
+    p01 = COLS ? lo.y : hi.x;
     p11 = hi.y;
   }
 };
+
+template <> struct SharedTaps<LOLA_STORE_F16Q> : SharedQuadF16<Layout<LOLA_STORE_F16Q>::kCols> {};
 
 template <> struct SharedTaps<LOLA_STORE_BF16Q> {
   static constexpr bool kQuad = true;
@@ -192,7 +195,8 @@ template <> struct SharedTaps<LOLA_STORE_BF16Q> {
   }
 };
 
-template <> struct SharedTaps<LOLA_STORE_F16QX> : SharedTaps<LOLA_STORE_F16Q> {};
+template <> struct SharedTaps<LOLA_STORE_F16QX>
+    : SharedQuadF16<Layout<LOLA_STORE_F16QX>::kCols> {};
 template <> struct SharedTaps<LOLA_STORE_F32QX>
     : SharedQuadF32<Layout<LOLA_STORE_F32QX>::kCols> {};
 
@@ -259,7 +263,7 @@ __device__ __forceinline__ void applyStagedPairs(const TileProj &tp, const unsig
   /* 2^23 + box-local index of pixel (cu, cv), which lies in the box (the tile
      origin's own pixel is inside its footprint) */
   const float kxc = fmaf(tp.cv + tp.syo, (float)g.boxW, tp.sxm + tp.cu);
-  pairedUpdate<VPT, KAHAN, SharedTaps<S>::kDiff, false>(tp, fi, fj, kxc, (float)g.boxW, fetch,
+  pairedUpdate<VPT, KAHAN, SharedTaps<S>::kDiff, 0u>(tp, fi, fj, kxc, (float)g.boxW, fetch,
       acc, comp);
 }
 
