@@ -66,9 +66,14 @@ METRIC = "GUPS (1e9 voxel updates/s) N=512,1024: FP16-stored vs FP32 path, RMSE 
 # MIXED_TEX_FRACTION of their voxels through the texture unit
 # (LOLA_MIXED_TEX_MASK = 0xAAAA in lolacuda_internal.h).  The 16-bit quad
 # layouts store bilinear terms, so their interpolation is 3 FMAs instead of 6
-# operations (3 issue slots less per voxel, 1.5 on the paired path).
+# operations (3 issue slots less per voxel, 1.5 on the paired path).  FP32
+# quads (f32q) are stored column by column and interpolated per voxel on the
+# paired path: 2 packed + 2 scalar instead of 3 packed per voxel (+1), in
+# exchange for the register moves the pairwise form needs (moves are not
+# counted for either form).
 MIXED_TEX_FRACTION = 0.5
 _TERM_LAYOUTS = ("f16q", "bf16q", "f16qx")
+_COLUMN_LAYOUTS = ("f32q",)
 _LOAD_FETCH = {"f32": 7, "f16": 11, "bf16": 11, "f32q": 4, "f16q": 8, "bf16q": 8}
 _TEX_FETCH = 3
 
@@ -88,7 +93,7 @@ def instr_per_update(storage, paired_fraction):
     fetch, load_frac = _fetch_cost(storage)
     terms = storage in _TERM_LAYOUTS
     one = (15 if terms else 18) + load_frac + fetch
-    two = (9.5 if terms else 11) + fetch
+    two = (9.5 if terms else 12 if storage in _COLUMN_LAYOUTS else 11) + fetch
     return paired_fraction * two + (1 - paired_fraction) * one
 
 
