@@ -212,8 +212,9 @@ int lolaCudaPlanDownloadVolume(LolaCudaPlan *plan, float *h_volume);
  * memory makes the call return at once).  The next host-staged pass takes up
  * to the edge batch of projections (LolaCudaConfig.edgeBatch). */
 int lolaCudaPlanUploadVolumeAsync(LolaCudaPlan *plan, const float *h_volume);
-/* Asks for the volume in h_volume after the next pass: that pass runs in
- * z-chunks and each chunk is copied out as soon as it is finished, so the
+/* Asks for the volume in h_volume after the last pass of the next
+ * backprojection call (lolaCudaPlanBackprojectHost / Device): that pass runs
+ * in z-chunks and each chunk is copied out as soon as it is finished, so the
  * download overlaps the pass.  If no pass runs first, lolaCudaPlanSynchronize
  * copies the volume as it is.  The copy is complete when
  * lolaCudaPlanSynchronize returns.  Results are identical to a whole pass

@@ -622,22 +622,23 @@ __device__ __forceinline__ void pairedUpdate(const TileProj &tp, float fi, float
       }
       VAL = make_float2(val[0], val[1]);
     } else {
-    float p00[2], p10[2], p01[2], p11[2];
+      /* pairwise: the two voxels' taps (or terms) packed slot by slot */
+      float p00[2], p10[2], p01[2], p11[2];
 #pragma unroll
-    for (int h = 0; h < 2; ++h)
-      fetch(2 * j + h, h ? IDX.y : IDX.x, h ? TX.y : TX.x, h ? TY.y : TY.x, p00[h], p10[h],
-          p01[h], p11[h]);
-    const float2 P00 = make_float2(p00[0], p00[1]), P10 = make_float2(p10[0], p10[1]);
-    const float2 P01 = make_float2(p01[0], p01[1]), P11 = make_float2(p11[0], p11[1]);
-    if (DIFF) {  /* terms: p00, p10 - p00, p01 - p00, p11 - p01 - p10 + p00 */
-      const float2 B = __ffma2_rn(AX, P10, P00);
-      const float2 C = __ffma2_rn(AX, P11, P01);
-      VAL = __ffma2_rn(AY, C, B);
-    } else {
-      const float2 B = __ffma2_rn(AX, __ffma2_rn(P00, neg1, P10), P00);
-      const float2 T = __ffma2_rn(AX, __ffma2_rn(P01, neg1, P11), P01);
-      VAL = __ffma2_rn(AY, __ffma2_rn(B, neg1, T), B);
-    }
+      for (int h = 0; h < 2; ++h)
+        fetch(2 * j + h, h ? IDX.y : IDX.x, h ? TX.y : TX.x, h ? TY.y : TY.x, p00[h], p10[h],
+            p01[h], p11[h]);
+      const float2 P00 = make_float2(p00[0], p00[1]), P10 = make_float2(p10[0], p10[1]);
+      const float2 P01 = make_float2(p01[0], p01[1]), P11 = make_float2(p11[0], p11[1]);
+      if (DIFF) {  /* terms: p00, p10 - p00, p01 - p00, p11 - p01 - p10 + p00 */
+        const float2 B = __ffma2_rn(AX, P10, P00);
+        const float2 C = __ffma2_rn(AX, P11, P01);
+        VAL = __ffma2_rn(AY, C, B);
+      } else {
+        const float2 B = __ffma2_rn(AX, __ffma2_rn(P00, neg1, P10), P00);
+        const float2 T = __ffma2_rn(AX, __ffma2_rn(P01, neg1, P11), P01);
+        VAL = __ffma2_rn(AY, __ffma2_rn(B, neg1, T), B);
+      }
     }
     const float2 RR = __fmul2_rn(R, R);
     if (KAHAN) {

@@ -918,11 +918,16 @@ int lolaCudaPlanBackprojectDevice(LolaCudaPlan *p, const float *d_images, size_t
   if (p->pending != 0)
     return setError("host-staged projections pending; synchronize the plan first");
   CUDA_TRY(cudaSetDevice(p->device));
+  /* a pending stream-out request belongs to the call's last pass */
+  float *out = p->streamOut;
+  p->streamOut = NULL;
   for (int done = 0; done < count;) {
     const int n = (count - done < p->cfg.batch) ? count - done : p->cfg.batch;
     LAUNCH_TRY(lolaLaunchPack(&p->store, d_images + (size_t)done * imageStride, imageStride,
         p->d_ring, 0, n, p->stream));
     p->stats.packs++;
+    if (done + n == count)
+      p->streamOut = out;
     if (!launchPass(p, h_mats + 12 * (size_t)done, n))
       return 0;
     done += n;
@@ -1005,17 +1010,23 @@ int lolaCudaPlanBackprojectHost(LolaCudaPlan *p, const float *h_images, size_t i
     return setError("null argument");
   CUDA_TRY(cudaSetDevice(p->device));
   int flushed = 0;
-  /* a call whose last pass streams the volume out is the end of its scan:
-     that pass takes the edge batch */
-  const int tail = p->streamOut != NULL;
+  /* a pending stream-out request belongs to this call's last pass, the end
+     of its scan: that pass takes the edge batch, and the call's earlier
+     passes leave the request alone */
+  float *out = p->streamOut;
+  p->streamOut = NULL;
   for (int i = 0; i < count; i++) {
-    p->scanLeft = tail ? count - i : 0;
+    p->scanLeft = out != NULL ? count - i : 0;
+    if (i == count - 1)
+      p->streamOut = out;
     if (!stageHost(p, h_images + (size_t)i * imageStride, h_mats + 12 * (size_t)i, &flushed)) {
       p->scanLeft = 0;
       return 0;
     }
   }
   p->scanLeft = 0;
+  if (count == 0)
+    p->streamOut = out;
   if (!flushPending(p))
     return 0;
   CUDA_TRY(cudaStreamSynchronize(p->copyStream));

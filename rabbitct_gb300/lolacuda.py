@@ -104,8 +104,9 @@ class Plan:
               "upload volume async")
 
     def stream_out(self, out: np.ndarray) -> np.ndarray:
-        """The volume lands in `out` after the next pass (or at synchronize()),
-        chunk by chunk as the pass finishes; complete after synchronize()."""
+        """The volume lands in `out` after the last pass of the next
+        backproject call (or at synchronize()), chunk by chunk as that pass
+        finishes; complete after synchronize()."""
         assert out.dtype == np.float32 and out.flags.c_contiguous
         assert out.size == self.n * self.n * self.slab[1]
         self._hold.append(out)

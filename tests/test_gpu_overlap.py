@@ -108,6 +108,41 @@ def test_first_pass_after_upload_takes_the_edge_batch(lib, scan7):
     assert np.array_equal(out, want)
 
 
+def test_stream_out_belongs_to_the_calls_last_pass(lib, scan7):
+    """A stream-out request made before a call of several passes delivers the
+    volume after the call's last pass.  From host images that last pass takes
+    the edge batch (4; batch 2: passes of 2, 1 and 4); from device images the
+    passes are batch-sized (3, 3, 1)."""
+    from rabbitct_gb300.lolacuda import DeviceBuffer, Plan
+    init = _initial(N, N, seed=10)
+    vs, o = _geom(N)
+    want = _sync_result(scan7, N, init, None, splits=(2, 3), batch=4)
+    out = np.full_like(init, np.nan)
+    with Plan(N, vs, o, scan7.width, scan7.height, batch=2, edge_batch=4,
+              collect_stats=1) as p:
+        p.upload(init)
+        p.stream_out(out)
+        p.backproject_host(scan7.images, scan7.matrices)
+        p.synchronize()
+        st = p.stats()
+    assert st.passes == 3 and st.overlappedPasses == 1
+    assert np.array_equal(out, want)
+    want = _sync_result(scan7, N, init, None, batch=3)
+    out = np.full_like(init, np.nan)
+    d_img = DeviceBuffer.from_array(np.ascontiguousarray(scan7.images, np.float32))
+    try:
+        with Plan(N, vs, o, scan7.width, scan7.height, batch=3, collect_stats=1) as p:
+            p.upload(init)
+            p.stream_out(out)
+            p.backproject_device(d_img.ptr, scan7.width * scan7.height, scan7.matrices)
+            p.synchronize()
+            st = p.stats()
+    finally:
+        d_img.free()
+    assert st.passes == 3 and st.overlappedPasses == 1
+    assert np.array_equal(out, want)
+
+
 def test_edge_batch_is_validated(lib):
     from rabbitct_gb300._native import LolaCudaError
     from rabbitct_gb300.lolacuda import Plan
