@@ -66,14 +66,15 @@ METRIC = "GUPS (1e9 voxel updates/s) N=512,1024: FP16-stored vs FP32 path, RMSE 
 # the gathers (4 plain or 1 quad) and 4 widenings of 16-bit taps on the load
 # path, or 2 coordinate adds and 1 texture gather.  Mixed layouts fetch
 # MIXED_TEX_FRACTION of their voxels through the texture unit
-# (LOLA_MIXED_TEX_MASK = 0xAAAA in lolacuda_internal.h).  The 16-bit quad
+# (LOLA_MIXED_COLS_TEX_MASK = 0xABAB for f16qx, LOLA_MIXED_TEX_MASK = 0xAAAA
+# for f32qx, in lolacuda_internal.h).  The 16-bit quad
 # layouts store bilinear terms, so their interpolation is 3 FMAs instead of 6
 # operations (3 issue slots less per voxel, 1.5 on the paired path).  FP32
 # quads (f32q) are stored column by column and interpolated per voxel on the
 # paired path: 2 packed + 2 scalar instead of 3 packed per voxel (+1), in
 # exchange for the register moves the pairwise form needs (moves are not
 # counted for either form).
-MIXED_TEX_FRACTION = 0.5
+MIXED_TEX_FRACTION = {"f16qx": 10 / 16, "f32qx": 0.5}  # LOLA_MIXED_(COLS_)TEX_MASK
 _TERM_LAYOUTS = ("f16q", "bf16q", "f16qx")
 _COLUMN_LAYOUTS = ("f32q",)
 _LOAD_FETCH = {"f32": 7, "f16": 11, "bf16": 11, "f32q": 4, "f16q": 8, "bf16q": 8}
@@ -86,7 +87,7 @@ def _fetch_cost(storage):
         return _TEX_FETCH, 0.0
     if storage in ("f16qx", "f32qx"):
         load = _LOAD_FETCH["f16q" if storage == "f16qx" else "f32q"]
-        t = MIXED_TEX_FRACTION
+        t = MIXED_TEX_FRACTION[storage]
         return t * _TEX_FETCH + (1 - t) * load, 1 - t
     return _LOAD_FETCH[storage], 1.0
 

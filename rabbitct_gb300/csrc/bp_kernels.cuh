@@ -361,20 +361,6 @@ __device__ __forceinline__ void texTaps(unsigned long long tex, float cx, float 
  * texture unit (a point fetch, widened to FP32 there), the others through the
  * load path, so both gather pipes work in parallel. */
 
-/* 1: f16qx stores its quads column by column, and its texture-read voxels
-   are paired in the texture mask LOLA_MIXED_COLS_TEX_MASK (both voxels of a
-   pair by texture or both by loads): a texel then lands as the two column
-   pairs that one packed FMA interpolates in x.  Measured on GB300 at N=1024:
-   1471 GUPS vs 1470 for the row order with mask 0xAAAA (and 1419 for the row
-   order with mask 0xCCCC, whose texture pairs need register moves), so the
-   default stays the row order */
-#ifndef LOLA_F16QX_COLS
-#define LOLA_F16QX_COLS 0
-#endif
-#ifndef LOLA_MIXED_COLS_TEX_MASK
-#define LOLA_MIXED_COLS_TEX_MASK 0xCCCCu
-#endif
-
 template <> struct Layout<LOLA_STORE_F16QX> : QuadF16Layout<LOLA_F16QX_COLS> {
   static constexpr bool kMixed = true;
 };

@@ -91,12 +91,28 @@ typedef struct {
  * skipped, fast (staged included), slow, staged, and fast on the paired path. */
 #define LOLA_TILE_COUNTERS 5
 
-/* Mixed layouts: voxels (bit k of each 8, per thread) that fetch through the
- * texture unit.  With the paired path (one load and one texture voxel per
- * pair) 4 of every 8 measured best on GB300: +2.5 % over 2 of 8, 4 % over 1
- * of 8 or none, 2 % over whole pairs through the texture unit. */
+/* Mixed layouts: voxels (bit k of a thread's column) that fetch through the
+ * texture unit.  Row-ordered quads (f32qx, and f16qx with LOLA_F16QX_COLS 0):
+ * with the paired path (one load and one texture voxel per pair) 4 of every
+ * 8 measured best on GB300: +2.5 % over 2 of 8, 4 % over 1 of 8 or none, 2 %
+ * over whole pairs through the texture unit. */
 #ifndef LOLA_MIXED_TEX_MASK
 #define LOLA_MIXED_TEX_MASK 0xAAAAu
+#endif
+
+/* 1: f16qx stores its quads column by column.  A texel then lands as the two
+ * column pairs that one packed FMA interpolates in x, so pairs read wholly
+ * through the texture unit need no register moves, and the pass kernel uses
+ * LOLA_MIXED_COLS_TEX_MASK: 10 of every 16 voxels by texture, one whole pair
+ * and three half pairs in each 8.  Measured on GB300 at N=1024 (f16qx GUPS):
+ * 1514-1518 vs 1468-1470 for the row order with 0xAAAA; with the column
+ * order 0x3B3B 1481, 0x2F2F 1463, 0x3F3F 1442, 0x0F0F 1399, 0xFFFF 1302; with
+ * the row order 0xABAB 1489-1491, 0xBABA 1485, 0xBBBB 1452, 0xFFFF 1297. */
+#ifndef LOLA_F16QX_COLS
+#define LOLA_F16QX_COLS 1
+#endif
+#ifndef LOLA_MIXED_COLS_TEX_MASK
+#define LOLA_MIXED_COLS_TEX_MASK 0xABABu
 #endif
 
 /* Stage buffers of the staged pass (a build-time tuning knob). */

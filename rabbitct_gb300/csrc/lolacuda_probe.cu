@@ -136,7 +136,10 @@ extern "C" double lolaCudaProbeGatherRate(int storage, int width, int height)
     const int elem = storage == LOLA_STORE_F16QX ? 8 : 16;
     const double lsu = probeKind(elem == 8 ? 3 : 2, elem, 1, width, height);
     const double tex = probeKind(5, elem, 4, width, height);
-    const double ft = __builtin_popcount(LOLA_MIXED_TEX_MASK & 0xFFu) / 8.0;
+    /* the pass kernel's texture share (PassTexMask in bp_kernels.cuh) */
+    const unsigned mask = (storage == LOLA_STORE_F16QX && LOLA_F16QX_COLS)
+                              ? LOLA_MIXED_COLS_TEX_MASK : LOLA_MIXED_TEX_MASK;
+    const double ft = __builtin_popcount(mask & 0xFFFFu) / 16.0;
     if (lsu <= 0.0 || tex <= 0.0)
       return -1.0;
     if (ft <= 0.0)
