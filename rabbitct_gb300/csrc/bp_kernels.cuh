@@ -202,8 +202,8 @@ template <> struct Layout<LOLA_STORE_BF16> {
 /* 1: FP32 quads are stored column by column, (p00, p01, p10, p11), so that a
    quad load lands as the two column pairs the paired path interpolates in
    x with one packed FMA each (f32q 1352 vs 1294 GUPS at N=1024 on GB300);
-   0: row by row, (p00, p10, p01, p11).  The mixed layout f32qx keeps the row
-   order, measured 2 % faster for it. */
+   0: row by row, (p00, p10, p01, p11).  The mixed layout f32qx has its own
+   switch, LOLA_F32QX_COLS. */
 #ifndef LOLA_F32Q_COLS
 #define LOLA_F32Q_COLS 1
 #endif
@@ -365,7 +365,7 @@ template <> struct Layout<LOLA_STORE_F16QX> : QuadF16Layout<LOLA_F16QX_COLS> {
   static constexpr bool kMixed = true;
 };
 
-template <> struct Layout<LOLA_STORE_F32QX> : QuadF32Layout<false> {
+template <> struct Layout<LOLA_STORE_F32QX> : QuadF32Layout<LOLA_F32QX_COLS> {
   static constexpr bool kMixed = true;
 };
 
@@ -641,8 +641,9 @@ __device__ __forceinline__ void pairedUpdate(const TileProj &tp, float fi, float
 
 /* Texture mask of a mixed layout in the pass kernel. */
 template <int S> struct PassTexMask {
-  static constexpr unsigned kValue = Layout<S>::kCols ? LOLA_MIXED_COLS_TEX_MASK
-                                                      : LOLA_MIXED_TEX_MASK;
+  static constexpr unsigned kValue = !Layout<S>::kCols ? LOLA_MIXED_TEX_MASK
+                                     : S == LOLA_STORE_F32QX ? LOLA_F32QX_COLS_TEX_MASK
+                                                             : LOLA_MIXED_COLS_TEX_MASK;
 };
 
 /* The paired update on the stored ring (loads, texture or both).  Voxels

@@ -115,6 +115,18 @@ typedef struct {
 #define LOLA_MIXED_COLS_TEX_MASK 0xABABu
 #endif
 
+/* 1: f32qx stores its quads column by column and the pass kernel uses
+ * LOLA_F32QX_COLS_TEX_MASK; 0: row order and LOLA_MIXED_TEX_MASK.  Measured
+ * on GB300 at N=1024, batch 32 (GUPS): row order 1196; column order with
+ * 0x2A2A 1231, 0x0303 1174, 0xABAB 1112, 0x2323 1081; all below f32q (1441),
+ * whose loads alone are faster than any share of 16-byte texels. */
+#ifndef LOLA_F32QX_COLS
+#define LOLA_F32QX_COLS 0
+#endif
+#ifndef LOLA_F32QX_COLS_TEX_MASK
+#define LOLA_F32QX_COLS_TEX_MASK 0xABABu
+#endif
+
 /* Stage buffers of the staged pass (a build-time tuning knob). */
 #ifndef LOLA_STAGES
 #define LOLA_STAGES 3

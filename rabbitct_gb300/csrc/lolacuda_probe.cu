@@ -137,8 +137,9 @@ extern "C" double lolaCudaProbeGatherRate(int storage, int width, int height)
     const double lsu = probeKind(elem == 8 ? 3 : 2, elem, 1, width, height);
     const double tex = probeKind(5, elem, 4, width, height);
     /* the pass kernel's texture share (PassTexMask in bp_kernels.cuh) */
-    const unsigned mask = (storage == LOLA_STORE_F16QX && LOLA_F16QX_COLS)
-                              ? LOLA_MIXED_COLS_TEX_MASK : LOLA_MIXED_TEX_MASK;
+    const unsigned mask = storage == LOLA_STORE_F16QX
+                              ? (LOLA_F16QX_COLS ? LOLA_MIXED_COLS_TEX_MASK : LOLA_MIXED_TEX_MASK)
+                              : (LOLA_F32QX_COLS ? LOLA_F32QX_COLS_TEX_MASK : LOLA_MIXED_TEX_MASK);
     const double ft = __builtin_popcount(mask & 0xFFFFu) / 16.0;
     if (lsu <= 0.0 || tex <= 0.0)
       return -1.0;
