@@ -865,7 +865,7 @@ template <int S, int VPT, int ROWS> struct MinBlocks {
 #define LOLA_PASS_MIN_BLOCKS(S, VPT, ROWS) (MinBlocks<S, VPT, ROWS>::kValue)
 #endif
 
-template <int S, int VPT, int ROWS, bool KAHAN>
+template <int S, int VPT, int ROWS, bool KAHAN, unsigned TEXMASK = PassTexMask<S>::kValue>
 __global__ void __launch_bounds__(32 * ROWS, LOLA_PASS_MIN_BLOCKS(S, VPT, ROWS))
     passKernel(const PassArgs a, const LolaPassParams P)
 {
@@ -932,7 +932,7 @@ __global__ void __launch_bounds__(32 * ROWS, LOLA_PASS_MIN_BLOCKS(S, VPT, ROWS))
     const void *img = static_cast<const char *>(a.ring) + (size_t)tp.slot * a.slotBytes;
     const unsigned long long tex =
         (Layout<S>::kTex || Layout<S>::kMixed) ? a.tex[tp.slot] : 0ull;
-    constexpr unsigned kMask = PassTexMask<S>::kValue;
+    constexpr unsigned kMask = TEXMASK;
     if (mode == MODE_FAST && tp.pos && LOLA_PAIRED)
       applyPairs<S, VPT, KAHAN, PassArgs, kMask>(tp, img, tex, a, fi, fj, acc, comp);
     else if (mode == MODE_FAST)
@@ -983,6 +983,15 @@ int launchPassShape(const PassArgs &a, const LolaPassParams *P, cudaStream_t str
   constexpr int TX = LOLA_WARP_X, TY = 32 * ROWS / TX;
   const dim3 grid((N + TX - 1) / TX, (N + TY - 1) / TY, (nz + VPT - 1) / VPT);
   (void)cudaGetLastError();
+  if constexpr (Layout<S>::kMixed && Layout<S>::kCols && VPT == 16 && ROWS == 4 &&
+                PassTexMask<S>::kValue != LOLA_MIXED_TEX_MASK) {
+    /* small volumes (N <= LOLA_COLS_MASK_MIN_N, coarse voxels) read fewer
+       voxels through the texture unit */
+    if (N <= LOLA_COLS_MASK_MIN_N) {
+      passKernel<S, VPT, ROWS, KAHAN, LOLA_MIXED_TEX_MASK><<<grid, block, 0, stream>>>(a, *P);
+      return (int)cudaGetLastError();
+    }
+  }
   passKernel<S, VPT, ROWS, KAHAN><<<grid, block, 0, stream>>>(a, *P);
   return (int)cudaGetLastError();
 }

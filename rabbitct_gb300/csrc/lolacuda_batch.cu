@@ -162,6 +162,11 @@ int chooseShapes(LolaCudaBatch *bt, const LolaCudaJob *jobs, const std::vector<L
   return 1;
 }
 
+/* 1: the branch passes read their projections from the batch's device table */
+#ifndef LOLA_BATCH_PROJ_DEVICE
+#define LOLA_BATCH_PROJ_DEVICE 1
+#endif
+
 int captureBranches(LolaCudaBatch *bt, const LolaCudaJob *jobs,
     const std::vector<LolaBatchJob> &hj, const std::vector<unsigned long long> &tex)
 {
@@ -189,6 +194,31 @@ int captureBranches(LolaCudaBatch *bt, const LolaCudaJob *jobs,
     BT_TRY(cudaStreamCreateWithFlags(&bt->branches[k], cudaStreamNonBlocking));
   for (int k = 0; k <= K; ++k)
     BT_TRY(cudaEventCreateWithFlags(&bt->events[k], cudaEventDisableTiming));
+
+  /* every job's projections in device memory, job after job, each with the
+     ring slot its wave packs it into: the passes' per-tile setup reads them
+     there (kernel-parameter reads from one lane per projection would be
+     served one address at a time) */
+  std::vector<size_t> first(nj + 1, 0);
+  for (int j = 0; j < nj; ++j)
+    first[j + 1] = first[j] + (size_t)(hj[j].nproj > 0 ? hj[j].nproj : 0);
+  if (first[nj] > 0) {
+    std::vector<LolaPassProj> all(first[nj]);
+    memset(all.data(), 0, all.size() * sizeof(LolaPassProj));
+    for (int j = 0; j < nj; ++j)
+      for (int k = 0; k < hj[j].nproj; ++k) {
+        const double *m = jobs[j].h_matrices + 12 * (size_t)k;
+        LolaPassProj &pp = all[first[j] + k];
+        memcpy(pp.a, m, 12 * sizeof(double));
+        for (int ax = 0; ax < 3; ++ax)
+          for (int c = 0; c < 3; ++c)
+            pp.step[ax][c] = (float)(m[ax * 3 + c] * (double)hj[j].voxelSize);
+        pp.slot = k % b;
+      }
+    BT_TRY(cudaMalloc(&bt->d_proj, all.size() * sizeof(LolaPassProj)));
+    BT_TRY(cudaMemcpy(bt->d_proj, all.data(), all.size() * sizeof(LolaPassProj),
+        cudaMemcpyHostToDevice));
+  }
 
   BT_TRY(cudaStreamBeginCapture(bt->stream, cudaStreamCaptureModeThreadLocal));
   cudaError_t e = cudaEventRecord(bt->events[K], bt->stream);
@@ -235,6 +265,7 @@ int captureBranches(LolaCudaBatch *bt, const LolaCudaJob *jobs,
               P.proj[i].step[ax][c] = (float)(m[ax * 3 + c] * (double)J.voxelSize);
           P.proj[i].slot = i;
         }
+        P.projDevice = LOLA_BATCH_PROJ_DEVICE ? bt->d_proj + first[j] + w0 : nullptr;
         rc = lolaLaunchBackproject(&sd, &P, nullptr, J.ring, J.volume, nullptr, st);
         bt->launches += 2;
       }

@@ -136,7 +136,8 @@ extern "C" double lolaCudaProbeGatherRate(int storage, int width, int height)
     const int elem = storage == LOLA_STORE_F16QX ? 8 : 16;
     const double lsu = probeKind(elem == 8 ? 3 : 2, elem, 1, width, height);
     const double tex = probeKind(5, elem, 4, width, height);
-    /* the pass kernel's texture share (PassTexMask in bp_kernels.cuh) */
+    /* the pass kernel's texture share (PassTexMask in bp_kernels.cuh; the
+       share of volumes above LOLA_COLS_MASK_MIN_N) */
     const unsigned mask = storage == LOLA_STORE_F16QX
                               ? (LOLA_F16QX_COLS ? LOLA_MIXED_COLS_TEX_MASK : LOLA_MIXED_TEX_MASK)
                               : (LOLA_F32QX_COLS ? LOLA_F32QX_COLS_TEX_MASK : LOLA_MIXED_TEX_MASK);
