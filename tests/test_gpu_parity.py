@@ -186,6 +186,27 @@ def test_fp32_quads_equal_plain_fp32(lib, storage):
         assert np.array_equal(vols[1], vols[0]), (vpt, rows)
 
 
+@pytest.mark.parametrize("n", [128, 640])
+def test_mixed_fp16_quads_equal_load_only_quads(lib, n):
+    """f16qx (column-ordered quads, some voxels through the texture unit: 8
+    of 16 up to N=512, 10 of 16 above) and f16q (row-ordered quads, loads
+    only) hold the same FP16 terms, and the texture's point fetch widens them
+    exactly: the volumes are identical on either side of the mask switch."""
+    from rabbitct_gb300.lolacuda import Plan
+    spec = synth.ScanSpec(nproj=4, seed=4)
+    scan = synth.make_scan(spec)
+    vs = synth.voxel_size(n)
+    o = synth.origin_index(n, vs)
+    vols = []
+    for storage in ("f16q", "f16qx"):
+        with Plan(n, vs, o, spec.width, spec.height, storage=storage, batch=4,
+                  collect_stats=1) as plan:
+            plan.backproject_host(scan.images, scan.matrices)
+            vols.append(plan.download())
+            assert plan.stats().tilePassesPaired > 0
+    assert np.array_equal(vols[1], vols[0])
+
+
 @pytest.mark.parametrize("batch_call", [1, 3])
 @pytest.mark.parametrize("with_geometry", [True, False])
 def test_module_api_like_runner(lib, scan12, batch_call, with_geometry):
