@@ -350,12 +350,14 @@ int lolaCudaSlab(int problemSize, int rank, int ranks, int align, int32_t *slice
  * default stream); the caller synchronises.  `config` may be NULL (defaults);
  * its batch is capped by what fits in the scratch.
  * Calls no cudaMalloc, cudaFree or other allocating routine: the packed
- * projections live in a fixed LOLA_NOALLOC_SCRATCH_BYTES device array that
- * every GPU loading this library holds until exit.  A packed projection larger
- * than that array is rejected with an error.  All calls share the array, so
- * calls whose work overlaps on the GPU race and must be serialised.  The
- * array's device address is looked up on the first call on each device: make
- * that call before any stream capture begins. */
+ * projections live in a fixed LOLA_NOALLOC_SCRATCH_BYTES device array, and
+ * each pass's projection records (LOLA_MAX_BATCH x 152 bytes) in a second,
+ * both held by every GPU loading this library until exit; a one-block kernel
+ * per pass fills the second from its launch parameters.  A packed projection
+ * larger than the first array is rejected with an error.  All calls share the
+ * arrays, so calls whose work overlaps on the GPU race and must be serialised.
+ * The arrays' device addresses are looked up on the first call on each device:
+ * make that call before any stream capture begins. */
 #define LOLA_NOALLOC_SCRATCH_BYTES (32u << 20)
 int lolaCudaBackprojectNoAlloc(const LolaCudaGeometry *geometry, const LolaCudaConfig *config,
     float *d_volume, const float *d_images, size_t imageStride, const double *h_matrices,

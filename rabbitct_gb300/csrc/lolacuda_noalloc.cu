@@ -6,9 +6,9 @@
  * framework that owns the device memory pool and forbids libraries from
  * allocating behind its back.  lolaCudaBackprojectNoAlloc serves them: the
  * caller passes the volume and the projections, already in device memory, and
- * the only scratch the operation needs — the ring of packed, zero-padded
- * projections that the pass kernel gathers from — is the fixed array below,
- * part of the library's device image.
+ * the scratch the operation needs — the ring of packed, zero-padded
+ * projections that the pass kernel gathers from, and each pass's projection
+ * records — are the fixed arrays below, part of the library's device image.
  *
  * Limits and sharing:
  *  - the scratch is LOLA_NOALLOC_SCRATCH_BYTES (32 MiB) on every GPU that
@@ -32,29 +32,50 @@
 #include "lolacuda_internal.h"
 
 static __device__ __align__(256) unsigned char gNoAllocScratch[LOLA_NOALLOC_SCRATCH_BYTES];
+/* the current pass's projections, where the per-tile setup reads them (from
+   the kernel parameters one lane per projection reads divergent addresses,
+   which the constant cache serves one at a time) */
+static __device__ LolaPassProj gNoAllocProj[LOLA_MAX_BATCH];
+
+/* Copies a pass's projections from its parameters into gNoAllocProj: a
+   kernel, so that the call stays free of host copies and capturable. */
+__global__ void __launch_bounds__(128) noAllocProjKernel(const __grid_constant__ LolaPassParams P,
+    LolaPassProj *dst)
+{
+  const int words = P.count * (int)(sizeof(LolaPassProj) / sizeof(uint32_t));
+  const uint32_t *src = reinterpret_cast<const uint32_t *>(P.proj);
+  uint32_t *d = reinterpret_cast<uint32_t *>(dst);
+  for (int i = threadIdx.x; i < words; i += blockDim.x)
+    d[i] = src[i];
+}
 
 namespace {
 
 constexpr int kMaxDevices = 64;
 void *gScratchAddr[kMaxDevices];
+LolaPassProj *gProjAddr[kMaxDevices];
 std::mutex gScratchMutex;
 
-/* Device address of gNoAllocScratch on `device` (the current device).  The
- * symbol's name in host code is only a host-side handle, so the address must
- * come from the runtime. */
-int scratchAddress(int device, void **out)
+/* Device addresses of gNoAllocScratch and gNoAllocProj on `device` (the
+ * current device).  The symbols' names in host code are only host-side
+ * handles, so the addresses must come from the runtime. */
+int scratchAddress(int device, void **out, LolaPassProj **proj)
 {
   if (device < 0 || device >= kMaxDevices)
     return lolaSetError("device ordinal %d above %d", device, kMaxDevices - 1);
   std::lock_guard<std::mutex> lock(gScratchMutex);
   if (gScratchAddr[device] == nullptr) {
-    void *p = nullptr;
-    const cudaError_t e = cudaGetSymbolAddress(&p, gNoAllocScratch);
+    void *p = nullptr, *q = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, gNoAllocScratch);
+    if (e == cudaSuccess)
+      e = cudaGetSymbolAddress(&q, gNoAllocProj);
     if (e != cudaSuccess)
       return lolaSetError("cudaGetSymbolAddress(no-alloc scratch): %s", cudaGetErrorString(e));
+    gProjAddr[device] = static_cast<LolaPassProj *>(q);
     gScratchAddr[device] = p;
   }
   *out = gScratchAddr[device];
+  *proj = gProjAddr[device];
   return 1;
 }
 
@@ -135,7 +156,8 @@ extern "C" int lolaCudaBackprojectNoAlloc(const LolaCudaGeometry *g, const LolaC
   if (e != cudaSuccess)
     return lolaSetError("cudaGetDevice: %s", cudaGetErrorString(e));
   void *ring = nullptr;
-  if (!scratchAddress(device, &ring))
+  LolaPassProj *projScratch = nullptr;
+  if (!scratchAddress(device, &ring, &projScratch))
     return 0;
 
   LolaPassParams P;
@@ -155,7 +177,7 @@ extern "C" int lolaCudaBackprojectNoAlloc(const LolaCudaGeometry *g, const LolaC
     P.voxelsPerThread = c.voxelsPerThread;
     P.rowsPerBlock = c.rowsPerBlock;
     P.countTiles = 0;
-    P.projDevice = nullptr;  /* projections from the kernel parameters */
+    P.projDevice = projScratch;
     for (int i = 0; i < n; i++) {
       const double *m = h_matrices + 12 * (size_t)(done + i);
       LolaPassProj &pp = P.proj[i];
@@ -167,6 +189,11 @@ extern "C" int lolaCudaBackprojectNoAlloc(const LolaCudaGeometry *g, const LolaC
       pp.slot = i;
       pp.reserved[0] = pp.reserved[1] = pp.reserved[2] = 0;
     }
+    (void)cudaGetLastError();
+    noAllocProjKernel<<<1, 128, 0, static_cast<cudaStream_t>(stream)>>>(P, projScratch);
+    rc = (int)cudaGetLastError();
+    if (rc != 0)
+      return lolaSetError("projection copy launch failed: %s", cudaGetErrorString((cudaError_t)rc));
     rc = lolaLaunchBackproject(&st, &P, nullptr, ring, d_volume, nullptr, stream);
     if (rc != 0)
       return lolaSetError("pass launch failed: %s", cudaGetErrorString((cudaError_t)rc));
