@@ -33,15 +33,27 @@ def test_config_validation(lib):
         assert lib.lolaCudaLastError()
 
 
+def test_edge_batch_validation(lib):
+    """The edge batch is 0 (twice the batch) or batch..32."""
+    from rabbitct_gb300._native import config
+    for batch, edge, ok in ((16, 0, True), (16, 16, True), (16, 32, True), (16, 15, False),
+                            (16, 33, False), (32, 0, True), (1, 1, True)):
+        c = config(batch=batch, edge_batch=edge, exit_on_error=0)
+        assert lib.lolaCudaSetConfig(C.byref(c)) == int(ok), (batch, edge)
+        if not ok:
+            assert b"edge batch" in lib.lolaCudaLastError()
+
+
 def test_environment_overrides(lib, monkeypatch):
     from rabbitct_gb300._native import LolaCudaConfig
     monkeypatch.setenv("LOLACUDA_STORAGE", "bf16q")
     monkeypatch.setenv("LOLACUDA_ACCUM", "kahan")
     monkeypatch.setenv("LOLACUDA_BATCH", "4")
     monkeypatch.setenv("LOLACUDA_EXIT", "0")
+    monkeypatch.setenv("LOLACUDA_EDGE_BATCH", "12")
     c = LolaCudaConfig()
     lib.lolaCudaDefaultConfig(C.byref(c))
-    assert (c.storage, c.accumulation, c.batch, c.exitOnError) == (5, 1, 4, 0)
+    assert (c.storage, c.accumulation, c.batch, c.exitOnError, c.edgeBatch) == (5, 1, 4, 0, 12)
 
 
 def test_module_api_errors_without_prepare(lib):
