@@ -82,7 +82,8 @@ typedef struct {
  * R warps spans LOLA_WARP_X x (32 R / LOLA_WARP_X) x voxels-per-thread voxels.
  * A compact patch keeps a warp's detector footprint compact: measured on
  * GB300 at N=1024, 8 x 4 beat 32 x 1 by 6-8 % for the four-tap layouts (f32
- * 1214 vs 1127 GUPS), 2 % for tex16, and was within 1 % for the quad layouts. */
+ * 1214 vs 1127 GUPS), 2 % for tex16, and was within 1 % for the quad layouts
+ * (f16qx with column-ordered quads: 16 x 2 warps 1516 vs 1514 GUPS). */
 #ifndef LOLA_WARP_X
 #define LOLA_WARP_X 8
 #endif
