@@ -343,12 +343,19 @@ int lolaCudaSlab(int problemSize, int rank, int ranks, int align, int32_t *slice
  * that cannot allocate device memory while they run — an acquisition loop
  * that reserves its device memory at start-up and must not stall on
  * cudaMalloc/cudaFree (which can synchronise the device), or a host framework
- * that owns the device memory pool.  Same result as lolaCudaPlanBackprojectDevice
- * into a caller-owned volume: d_volume (N^3 FP32, x fastest) += the `count`
- * FP32 projections at d_images[p * imageStride + j * W + i] with host matrices
- * h_matrices[p * 12 + ...].  Enqueued on `stream` (a cudaStream_t, NULL = the
- * default stream); the caller synchronises.  `config` may be NULL (defaults);
- * its batch is capped by what fits in the scratch.
+ * that owns the device memory pool.  Same result, bit for bit, as
+ * lolaCudaPlanBackprojectDevice with the same batch into a caller-owned
+ * volume: d_volume (N x N x sliceCount FP32, x fastest; the geometry's slab
+ * fields as for a plan, 0 / 0 = the whole N^3 volume) += the `count` FP32
+ * projections at d_images[p * imageStride + j * W + i] with host matrices
+ * h_matrices[p * 12 + ...].  Enqueued on `stream` (a cudaStream_t of the
+ * current device, NULL = its default stream); the caller synchronises.  Runs
+ * on the calling thread's current device: config->device is not used.
+ * `config` may be NULL (defaults); its batch is capped by what fits in the
+ * scratch.  Storages: f32, f16, bf16, f32q, f16q, bf16q; f16qx and f32qx run
+ * as f16q and f32q (the same values, by loads only); tex32 and tex16 are
+ * rejected.  Projections per pass at 1248x960: f32 5, f16/bf16 10,
+ * f16q/bf16q 2, f32q 1 (the default storage).
  * Calls no cudaMalloc, cudaFree or other allocating routine: the packed
  * projections live in a fixed LOLA_NOALLOC_SCRATCH_BYTES device array, and
  * each pass's projection records (LOLA_MAX_BATCH x 152 bytes) in a second,
@@ -356,8 +363,9 @@ int lolaCudaSlab(int problemSize, int rank, int ranks, int align, int32_t *slice
  * per pass fills the second from its launch parameters.  A packed projection
  * larger than the first array is rejected with an error.  All calls share the
  * arrays, so calls whose work overlaps on the GPU race and must be serialised.
- * The arrays' device addresses are looked up on the first call on each device:
- * make that call before any stream capture begins. */
+ * The arrays' device addresses are looked up on the first call in each CUDA
+ * context (each device's primary context, normally): make that call before
+ * any stream capture begins, and do not reset the device between calls. */
 #define LOLA_NOALLOC_SCRATCH_BYTES (32u << 20)
 int lolaCudaBackprojectNoAlloc(const LolaCudaGeometry *geometry, const LolaCudaConfig *config,
     float *d_volume, const float *d_images, size_t imageStride, const double *h_matrices,

@@ -86,23 +86,25 @@ def _build_synth(force: bool = False) -> Path:
     return out
 
 
-def _build_lolacuda(force: bool = False, jobs: int | None = None) -> Path:
+def _build_lolacuda(force: bool = False, jobs: int | None = None, variant: str = "",
+                    variant_flags: tuple[str, ...] = ()) -> Path:
     LIB.mkdir(exist_ok=True)
-    OBJ.mkdir(exist_ok=True)
+    obj_dir = OBJ if not variant else PKG / f"_build_{variant}"
+    obj_dir.mkdir(exist_ok=True)
     cuda = _cuda_home()
     nvcc = str(cuda / "bin" / "nvcc")
-    out = LIB / "liblolacuda.so"
+    out = LIB / (f"liblolacuda_{variant}.so" if variant else "liblolacuda.so")
     headers = [CSRC / "bp_kernels.cuh", CSRC / "bp_staged.cuh", CSRC / "bp_batch.cuh",
                CSRC / "lolacuda_internal.h",
                INCLUDE / "lolaCuda.h"]
     common_inc = ["-I" + str(INCLUDE), "-I" + str(CSRC)]
 
     # extra nvcc flags for tuning builds, e.g. LOLACUDA_NVCC_FLAGS=-DLOLA_MIN_BLOCKS=5
-    extra = os.environ.get("LOLACUDA_NVCC_FLAGS", "").split()
+    extra = os.environ.get("LOLACUDA_NVCC_FLAGS", "").split() + list(variant_flags)
 
     def compile_cu(name: str) -> Path:
         src = CSRC / name
-        obj = OBJ / (name + ".o")
+        obj = obj_dir / (name + ".o")
         if force or _stale(obj, [src] + headers):
             _run([nvcc, *ARCH, "-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC",
                   *extra, *common_inc, "-c", str(src), "-o", str(obj)])
@@ -113,7 +115,7 @@ def _build_lolacuda(force: bool = False, jobs: int | None = None) -> Path:
 
     def compile_c(name: str) -> Path:
         src = CSRC / name
-        obj = OBJ / (name + ".o")
+        obj = obj_dir / (name + ".o")
         if force or _stale(obj, [src] + headers):
             # no contraction: host arithmetic rounds alike on x86 and Arm
             _run(["gcc", "-O2", "-std=c99", "-fPIC", "-ffp-contract=off", "-Wall", "-Wextra",
@@ -142,9 +144,10 @@ def _build_oracle(force: bool = False) -> Path:
     if force:
         _run(["make", "-C", str(oracle), "clean"])
     _run(["make", "-C", str(oracle)])
-    ref = Path(os.environ.get("RABBITCT_REFERENCE", "/root/reference"))
-    if (ref / "src" / "LolaBunny.c").exists():
-        _run(["make", "-C", str(REPO), "-f", "oracle/ref.mk", f"REF={ref}"])
+    from oracle import refpath
+    if refpath.present():
+        _run(["make", "-C", str(REPO), "-f", "oracle/ref.mk",
+              f"REF={refpath.reference_root()}"])
     return oracle / "liboracle.so"
 
 
@@ -159,6 +162,23 @@ def build_lolacuda(force: bool = False, jobs: int | None = None) -> Path:
     code, compiled in parallel; only stale objects are rebuilt."""
     with _BuildLock():
         return _build_lolacuda(force, jobs)
+
+
+# Test-only builds of the library, each with its own objects and file name.
+#  stagetimeout: the staged pass's producer issues no tensor copies and every
+#  mbarrier wait gives up after 200 000 clock cycles, so each wait runs out
+#  and the kernel's error path (error flag, abandoned stages, normal return)
+#  can be tested without a fault or a hang (tests/test_gpu_stage_timeout.py).
+VARIANTS = {
+    "stagetimeout": ("-DLOLA_STAGE_ISSUE_COPIES=0", "-DLOLA_STAGE_WAIT_CYCLES=200000ll"),
+}
+
+
+def build_lolacuda_variant(name: str, force: bool = False, jobs: int | None = None) -> Path:
+    """A test-only build of liblolacuda (VARIANTS[name]) as
+    _lib/liblolacuda_<name>.so; the product library is not touched."""
+    with _BuildLock():
+        return _build_lolacuda(force, jobs, variant=name, variant_flags=VARIANTS[name])
 
 
 def build_oracle(force: bool = False) -> Path:

@@ -42,7 +42,21 @@ struct StageArgs {
   int *errorFlag;
 };
 
-constexpr long long kWaitLimitCycles = 2000000000ll; /* about 1 s at 2 GHz */
+/* Clock budget of every mbarrier wait: about 1 s at 2 GHz. */
+#ifndef LOLA_STAGE_WAIT_CYCLES
+#define LOLA_STAGE_WAIT_CYCLES 2000000000ll
+#endif
+constexpr long long kWaitLimitCycles = LOLA_STAGE_WAIT_CYCLES;
+
+/* 1: the producer issues the tensor copies.  0 is for the wait-timeout test
+   build only (tests/test_gpu_stage_timeout.py, with a short
+   LOLA_STAGE_WAIT_CYCLES): the producer issues neither the copies nor their
+   byte counts, so no copy is ever in flight, every stage's full barrier stays
+   incomplete and each consumer warp's bounded wait runs out, records its
+   error code and abandons the staged work. */
+#ifndef LOLA_STAGE_ISSUE_COPIES
+#define LOLA_STAGE_ISSUE_COPIES 1
+#endif
 
 __device__ __forceinline__ uint32_t smemAddr(const void *p)
 {
@@ -353,9 +367,11 @@ __global__ void __launch_bounds__(32 * (ROWS + 1), LOLA_STAGED_MIN_BLOCKS)
           atomicExch(g.errorFlag, 1);
           break;
         }
-        mbarExpectTx(full0 + 8 * s, (uint32_t)g.boxBytes);
-        tmaLoad3d(smemAddr(stageMem + s * g.stageBytes), &tmap, t.bx * g.elemsPerPixel, t.by,
-            t.slot, full0 + 8 * s);
+        if (LOLA_STAGE_ISSUE_COPIES) {
+          mbarExpectTx(full0 + 8 * s, (uint32_t)g.boxBytes);
+          tmaLoad3d(smemAddr(stageMem + s * g.stageBytes), &tmap, t.bx * g.elemsPerPixel, t.by,
+              t.slot, full0 + 8 * s);
+        }
       }
     }
     return;

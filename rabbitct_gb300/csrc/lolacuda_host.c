@@ -1297,7 +1297,7 @@ int lolaCudaBackprojection(RabbitCtGlobalData *d)
     setError("cudaSetDevice failed");
     return moduleFail("backprojection");
   }
-  int flushed = 0;
+  int flushed = 0, closesScan = 0;
   for (uint32_t i = 0; i < d->numberOfProjections; i++) {
     const Projection *pr = &d->projectionBuffer[i];
     if (pr->image == NULL || pr->matrix == NULL) {
@@ -1322,13 +1322,17 @@ int lolaCudaBackprojection(RabbitCtGlobalData *d)
         return moduleFail("backprojection");
       flushed = 1;
     }
+    closesScan |= last;
   }
   /* the runner reuses its buffers after we return (src/rabbitRunner.c:275-278) */
   if (cudaStreamSynchronize(p->copyStream) != cudaSuccess) {
     setError("upload failed: %s", cudaGetErrorString(cudaGetLastError()));
     return moduleFail("backprojection");
   }
-  if (flushed && p->cfg.syncEachCall) {
+  /* the call that closes the scan waits for every pass even without
+     syncEachCall: the runner's timer around the calls then covers all of the
+     backprojection work, whatever the earlier calls left running */
+  if (flushed && (p->cfg.syncEachCall || closesScan)) {
     cudaError_t e = cudaStreamSynchronize(p->stream);
     if (e != cudaSuccess) {
       setError("pass failed: %s", cudaGetErrorString(e));
@@ -1351,6 +1355,14 @@ int lolaCudaFinish(RabbitCtGlobalData *d)
     return moduleFail("finish");
   }
   LolaCudaPlan *p = gPlan;
+  /* without the scan length (no -a) the last call cannot know it is the last,
+     so its pass runs here, outside the runner's timer: say so */
+  if (p->pending > 0 && gTotalProjections == 0) {
+    fprintf(stderr, "LolaCUDA finish: the last %d projection(s) were backprojected in finish, "
+                    "outside the timed calls (run with -a to close the scan in its last call)\n",
+        p->pending);
+    fflush(stderr);
+  }
   /* unless the last pass already streamed the volume out, the closing pass
      (or, with none pending, a plain copy) delivers it */
   if ((p->pending > 0 || p->outValid != d->volumeData) &&

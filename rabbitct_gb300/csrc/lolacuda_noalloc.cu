@@ -13,16 +13,25 @@
  * Limits and sharing:
  *  - the scratch is LOLA_NOALLOC_SCRATCH_BYTES (32 MiB) on every GPU that
  *    loads the library, held until the process exits;
- *  - one packed projection must fit in it (for FP32 storage about 6 MB at
- *    1248x960); as many as fit, up to the configured batch, share a pass;
+ *  - one packed projection must fit in it; as many as fit, up to the
+ *    configured batch, share a pass.  At 1248x960 (1376x1088 padded): FP32
+ *    taps 6.0 MB (5 per pass), FP16/BF16 taps 3.0 MB (10), FP16/BF16 quads
+ *    12 MB (2), FP32 quads 24 MB (1: the library's default storage, so a
+ *    call with config NULL runs one pass per projection);
+ *  - the storages read by loads only: f32, f16, bf16, f32q, f16q, bf16q.
+ *    f16qx and f32qx run as f16q and f32q (the same values, read by loads
+ *    only); tex32 and tex16 are rejected (they need texture objects);
  *  - every call uses the same array.  The pack kernel rewrites every element
  *    of each ring slot, zero margin included, before a pass reads it, so no
  *    state carries over from the previous call; but two calls whose work
  *    overlaps on the GPU (different streams, or different host threads on one
  *    device) race on the array and must be serialised by the caller.
- *  - the device address of the array is looked up once per device, on the
- *    first call made with that device current; make that first call before
- *    any stream capture begins.
+ *  - the device addresses of the arrays are looked up once per CUDA context
+ *    (normally once per device, the device's primary context), on the first
+ *    call made with it current; make that first call before any stream
+ *    capture begins.  A context destroyed and recreated at the same handle
+ *    (cudaDeviceReset) keeps the stale addresses: do not reset the device
+ *    between calls.
  */
 #include <mutex>
 
@@ -51,31 +60,88 @@ __global__ void __launch_bounds__(128) noAllocProjKernel(const __grid_constant__
 
 namespace {
 
-constexpr int kMaxDevices = 64;
-void *gScratchAddr[kMaxDevices];
-LolaPassProj *gProjAddr[kMaxDevices];
+typedef CUresult (*CtxGetCurrentFn)(CUcontext *);
+
+/* cuCtxGetCurrent through the runtime's driver entry points (no -lcuda). */
+CtxGetCurrentFn ctxGetCurrent()
+{
+  static CtxGetCurrentFn fn = nullptr;
+  static bool tried = false;
+  if (!tried) {
+    tried = true;
+    void *f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<CtxGetCurrentFn>(f);
+  }
+  return fn;
+}
+
+/* One entry per (device, context) the entry point ran in. */
+struct ScratchAddr {
+  int device;
+  CUcontext ctx;
+  void *ring;
+  LolaPassProj *proj;
+};
+constexpr int kMaxContexts = 64;
+ScratchAddr gAddr[kMaxContexts];
+int gAddrCount = 0;
 std::mutex gScratchMutex;
 
-/* Device addresses of gNoAllocScratch and gNoAllocProj on `device` (the
- * current device).  The symbols' names in host code are only host-side
- * handles, so the addresses must come from the runtime. */
+CUcontext currentContext()
+{
+  CUcontext ctx = nullptr;
+  CtxGetCurrentFn get = ctxGetCurrent();
+  if (get == nullptr || get(&ctx) != CUDA_SUCCESS)
+    return nullptr;
+  return ctx;
+}
+
+/* Address pair cached for (device, ctx); the mutex is held. */
+const ScratchAddr *findAddress(int device, CUcontext ctx)
+{
+  for (int i = 0; i < gAddrCount; i++)
+    if (gAddr[i].device == device && gAddr[i].ctx == ctx)
+      return &gAddr[i];
+  return nullptr;
+}
+
+/* Device addresses of gNoAllocScratch and gNoAllocProj in the current context
+ * of `device`.  The symbols' names in host code are only host-side handles,
+ * so the addresses must come from the runtime (cudaGetSymbolAddress), once
+ * per context.  A thread with no context bound yet (ctx null) gets the
+ * device's primary context bound by that lookup, and then finds the entry
+ * another thread made for it. */
 int scratchAddress(int device, void **out, LolaPassProj **proj)
 {
-  if (device < 0 || device >= kMaxDevices)
-    return lolaSetError("device ordinal %d above %d", device, kMaxDevices - 1);
   std::lock_guard<std::mutex> lock(gScratchMutex);
-  if (gScratchAddr[device] == nullptr) {
+  CUcontext ctx = currentContext();
+  const ScratchAddr *a = ctx != nullptr ? findAddress(device, ctx) : nullptr;
+  if (a == nullptr) {
     void *p = nullptr, *q = nullptr;
     cudaError_t e = cudaGetSymbolAddress(&p, gNoAllocScratch);
     if (e == cudaSuccess)
       e = cudaGetSymbolAddress(&q, gNoAllocProj);
     if (e != cudaSuccess)
       return lolaSetError("cudaGetSymbolAddress(no-alloc scratch): %s", cudaGetErrorString(e));
-    gProjAddr[device] = static_cast<LolaPassProj *>(q);
-    gScratchAddr[device] = p;
+    ctx = currentContext();
+    a = findAddress(device, ctx);
+    if (a == nullptr) {
+      if (gAddrCount == kMaxContexts)
+        return lolaSetError("no-alloc entry point used in more than %d contexts", kMaxContexts);
+      ScratchAddr &n = gAddr[gAddrCount++];
+      n.device = device;
+      n.ctx = ctx;
+      n.ring = p;
+      n.proj = static_cast<LolaPassProj *>(q);
+      a = &n;
+    }
   }
-  *out = gScratchAddr[device];
-  *proj = gProjAddr[device];
+  *out = a->ring;
+  *proj = a->proj;
   return 1;
 }
 
@@ -112,6 +178,16 @@ extern "C" int lolaCudaBackprojectNoAlloc(const LolaCudaGeometry *g, const LolaC
         g->imageHeight);
   if (!(g->voxelSize > 0.0f))
     return lolaSetError("voxel size must be positive");
+  /* the mixed layouts' values are their load-only layouts' (bit for bit); the
+     texture layouts need texture objects, which this entry point does not make */
+  if (c.storage == LOLA_STORE_F16QX)
+    c.storage = LOLA_STORE_F16Q;
+  else if (c.storage == LOLA_STORE_F32QX)
+    c.storage = LOLA_STORE_F32Q;
+  if (c.storage == LOLA_STORE_TEX32 || c.storage == LOLA_STORE_TEX16)
+    return lolaSetError("storage %s needs texture objects; the no-allocation entry point "
+                        "reads f32, f16, bf16, f32q, f16q, bf16q (f16qx, f32qx as f16q, f32q)",
+        c.storage == LOLA_STORE_TEX32 ? "tex32" : "tex16");
   const int eb = elemBytes(c.storage);
   if (eb == 0)
     return lolaSetError("invalid storage %d", c.storage);
@@ -120,6 +196,14 @@ extern "C" int lolaCudaBackprojectNoAlloc(const LolaCudaGeometry *g, const LolaC
   if (!lolaKernelShapeSupported(c.voxelsPerThread, c.rowsPerBlock))
     return lolaSetError("no kernel for %d voxels per thread x %d rows per block",
         c.voxelsPerThread, c.rowsPerBlock);
+  /* z-slab of the volume held in d_volume (N x N x sliceCount), as for a plan:
+     0 / 0 is the whole volume */
+  int zBegin = g->sliceBegin, zCount = g->sliceCount;
+  if (zBegin == 0 && zCount == 0)
+    zCount = g->problemSize;
+  if (zBegin < 0 || zCount <= 0 || zBegin + zCount > g->problemSize)
+    return lolaSetError("slab [%d, %d) outside the %d slices", g->sliceBegin,
+        g->sliceBegin + g->sliceCount, g->problemSize);
   if (count == 0)
     return 1;
   if (d_volume == nullptr || d_images == nullptr || h_matrices == nullptr)
@@ -132,13 +216,14 @@ extern "C" int lolaCudaBackprojectNoAlloc(const LolaCudaGeometry *g, const LolaC
   st.margin = LOLA_MARGIN;
   st.width = g->imageWidth;
   st.height = g->imageHeight;
-  st.pitch = g->imageWidth + 2 * LOLA_MARGIN;
+  /* the plan's layout: pitch a multiple of 32 pixels, slots 256 pixels apart */
+  st.pitch = (g->imageWidth + 2 * LOLA_MARGIN + 31) & ~31;
   st.rows = g->imageHeight + 2 * LOLA_MARGIN;
   st.reserved = 0;
   if ((long long)st.pitch * st.rows >= (1LL << 23) - 2 * (long long)st.pitch)
     return lolaSetError("detector %dx%d too large (padded image must stay below 2^23 pixels)",
         g->imageWidth, g->imageHeight);
-  st.slotElems = ((size_t)st.pitch * (size_t)st.rows + 63) & ~(size_t)63;
+  st.slotElems = ((size_t)st.pitch * (size_t)st.rows + 255) & ~(size_t)255;
   const size_t slotBytes = st.slotElems * (size_t)eb;
   if (slotBytes > LOLA_NOALLOC_SCRATCH_BYTES)
     return lolaSetError("one packed %dx%d projection needs %zu bytes; the no-allocation "
@@ -169,8 +254,8 @@ extern "C" int lolaCudaBackprojectNoAlloc(const LolaCudaGeometry *g, const LolaC
       return lolaSetError("pack launch failed: %s", cudaGetErrorString((cudaError_t)rc));
     P.N = g->problemSize;
     P.count = n;
-    P.zBegin = 0;
-    P.zEnd = g->problemSize;
+    P.zBegin = zBegin;
+    P.zEnd = zBegin + zCount;
     P.voxelSize = g->voxelSize;
     P.originIndex = g->originIndex;
     P.accumulation = c.accumulation;

@@ -1,6 +1,6 @@
 """Generates the golden fixtures from the reference RabbitCT itself.
 
-Needs the reference source tree (default /root/reference, or $RABBITCT_REFERENCE):
+Needs the reference source tree ($RABBITCT_REFERENCE, or oracle/refpath.py's default):
 it builds the unmodified reference into oracle/_ref (oracle/ref.mk) and runs
 
   - LolaBunny and LolaOPT through their module API (src/LolaBunny.c,
@@ -36,12 +36,12 @@ HERE = Path(__file__).resolve().parent
 ROOT = HERE.parent.parent
 sys.path.insert(0, str(ROOT))
 
-from oracle import oracle  # noqa: E402
+from oracle import oracle, refpath  # noqa: E402
 from rabbitct_gb300 import rct, synth  # noqa: E402
 from rabbitct_gb300.lolacuda import GlobalData, module_functions  # noqa: E402
 from rabbitct_gb300.runner import run_module  # noqa: E402
 
-REF = Path(os.environ.get("RABBITCT_REFERENCE", "/root/reference"))
+REF = refpath.reference_root()
 
 
 class OutShadow(C.Structure):

@@ -10,9 +10,11 @@ from pathlib import Path
 
 import pytest
 
+from oracle import refpath
+
 ROOT = Path(__file__).resolve().parent.parent
 HEADER = ROOT / "include" / "lolaCuda.h"
-REF_HEADER = Path("/root/reference/src/rabbitCt.h")
+REF_HEADER = refpath.reference_root() / "src" / "rabbitCt.h"
 
 
 @pytest.fixture(scope="module")

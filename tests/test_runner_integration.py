@@ -19,10 +19,11 @@ from pathlib import Path
 import numpy as np
 import pytest
 
+from oracle import refpath
 from rabbitct_gb300 import rct, synth
 
 ROOT = Path(__file__).resolve().parent.parent
-REF = Path(os.environ.get("RABBITCT_REFERENCE", "/root/reference"))
+REF = refpath.reference_root()
 RUNNER = ROOT / "oracle" / "_ref" / "rabbitRunnerLolaCUDA"
 
 
