@@ -1,7 +1,7 @@
 """ORACLE — test infrastructure only.
 
-ctypes front end of oracle/liboracle.so (the CPU restatements in oracle.c and
-oracle_opt.c) and of oracle/_ref/libref.so (the reference built from its own
+ctypes front end of oracle/liboracle.so (the CPU restatements in oracle.c,
+oracle_opt.c and oracle_asm.c) and of oracle/_ref/libref.so (the reference built from its own
 sources by oracle/ref.mk, present only where the reference tree is).  Only
 tests/, __graft_entry__.smoke() and bench.py's CPU-baseline arm import this.
 """
@@ -47,6 +47,11 @@ def lib() -> C.CDLL:
         L.oracleOptBackproject.argtypes = [C.c_int, C.c_float, C.c_float, C.c_int, _P, _P, _P,
                                            C.c_int, C.c_int, _P, _P]
         L.oracleOptBackproject.restype = None
+        L.oracleAsmPadding.argtypes = [_P, C.c_int, C.c_int, C.c_int, _P, _P]
+        L.oracleAsmPadding.restype = C.c_int
+        L.oracleAsmBackproject.argtypes = [C.c_int, C.c_float, C.c_float, C.c_int, _P, _P, _P,
+                                           C.c_int, C.c_int, _P, C.c_int, _P]
+        L.oracleAsmBackproject.restype = None
         L.oracleBunnyPoints.argtypes = geo + [_P, C.c_int, _P, C.c_int, _P]
         L.oracleBunnyPoints.restype = None
         L.oracleThreads.argtypes = []
@@ -138,6 +143,50 @@ class OptBaseline:
         lib().oracleOptBackproject(self.n, self.vs, self.o, len(ids), idarr.ctypes.data,
                                    mats.ctypes.data, ptrs, self.start, self.line,
                                    self.ranges.ctypes.data, vol.ctypes.data)
+
+
+class AsmBaseline:
+    """The LolaASM restatement (oracle_asm.c) set up like lolaAsmPrepare
+    (src/LolaASM.c:26-70): line ranges over all views widened to the vector
+    width, padding from the shadow rounded up to it.  Each call copies its
+    views into zero-padded buffers (src/LolaASM.c:113-122) and backprojects
+    them, y-blocked by 8 with the call's views inside each block."""
+
+    def __init__(self, n, vs, o, mats, w, h, vector_size=4, ranges=None):
+        self.n, self.vs, self.o, self.w, self.h = n, vs, o, w, h
+        self.vec = vector_size
+        self.mats = np.ascontiguousarray(mats, np.float64).reshape(-1, 12)
+        # the same table LolaOPT uses (computeLineRanges with this vector size)
+        self.ranges = (line_ranges(n, vs, o, self.mats, w, h, vector_size, signed_hit=False)
+                       if ranges is None else ranges)
+        sh = np.array(shadow(n, vs, o, self.mats, w, h), np.int32)
+        pad = np.zeros(4, np.int32)
+        rows = C.c_int(0)
+        self.line = lib().oracleAsmPadding(sh.ctypes.data, w, h, vector_size, pad.ctypes.data,
+                                           C.addressof(rows))
+        self.pad = pad
+        self.rows = rows.value
+        self.start = int(pad[2] * self.line + pad[0])
+        self._bufs: list[np.ndarray] = []
+
+    def backproject(self, vol: np.ndarray, ids, images) -> None:
+        # two zero rows past the padded image: LolaASM's top pad, abs(Vmax) - H
+        # (src/LolaASM.c:48), leaves no row for the second tap of a voxel that
+        # projects into the last padded row, and its row kernel also runs over
+        # voxels outside a row's range; the reference reads whatever follows
+        # its buffer there, this restatement reads zeros
+        while len(self._bufs) < len(ids):
+            self._bufs.append(np.zeros((self.rows + 2, self.line), np.float32))
+        ptrs = (C.c_void_p * len(ids))()
+        r0, c0 = int(self.pad[2]), int(self.pad[0])
+        for i, img in enumerate(images):
+            self._bufs[i][r0:r0 + self.h, c0:c0 + self.w] = img
+            ptrs[i] = self._bufs[i].ctypes.data
+        idarr = np.ascontiguousarray(ids, np.int32)
+        mats = np.ascontiguousarray(self.mats[idarr - 1])
+        lib().oracleAsmBackproject(self.n, self.vs, self.o, len(ids), idarr.ctypes.data,
+                                   mats.ctypes.data, ptrs, self.start, self.line,
+                                   self.ranges.ctypes.data, self.vec, vol.ctypes.data)
 
 
 def threads() -> int:

@@ -5,6 +5,9 @@ it builds the unmodified reference into oracle/_ref (oracle/ref.mk) and runs
 
   - LolaBunny and LolaOPT through their module API (src/LolaBunny.c,
     src/LolaOPT.c), driven like src/rabbitRunner.c drives them;
+  - LolaASM (src/LolaASM.c with its SIMD row kernel) the same way on the
+    full-field case, in a process of its own (`--asm-case NAME` writes
+    NAME_asm.npz from NAME.npz's inputs);
   - computeLineRanges and computeShadowOfProjection (src/analyseGeometry.c);
   - the reference runner binary end to end on a .rct file (N=128, the
     runner's smallest size), including its -c verification printout, its
@@ -17,6 +20,7 @@ the images so a change of the generator is detected instead of silently
 changing the inputs.
 
     python tests/golden/make_golden.py
+    python tests/golden/make_golden.py --asm-case bunny_n32   # one LolaASM fixture
 """
 from __future__ import annotations
 
@@ -152,7 +156,25 @@ def runner_case(tmp):
     print("runner_n128:", printed)
 
 
+def asm_case(name):
+    """The reference's LolaASM on a small case's inputs -> {name}_asm.npz.  One
+    process per case: lolaAsmBackprojection keeps its padded buffers in static
+    state sized by the first call (src/LolaASM.c:92-105), never reset."""
+    lib = oracle.ref_lib()
+    g = np.load(HERE / f"{name}.npz")
+    n, vs, o = int(g["n"]), float(g["voxel_size"]), float(g["origin_index"])
+    with tempfile.TemporaryDirectory() as tmp:
+        vol = run_module(module_functions(lib, "lolaAsm"), n, vs, o, g["matrices"], g["images"],
+                         batch=1, clip_filename=os.path.join(tmp, f"asm_{name}.rct")).volume
+    vec = 8 if os.uname().machine == "x86_64" else 4
+    np.savez_compressed(HERE / f"{name}_asm.npz", asm=vol, asm_vector_size=vec)
+    print(f"{name}_asm: LolaASM, vector size {vec}")
+
+
 def main():
+    if len(sys.argv) == 3 and sys.argv[1] == "--asm-case":
+        asm_case(sys.argv[2])
+        return
     if not (REF / "src" / "LolaBunny.c").exists():
         sys.exit(f"reference sources not found under {REF}")
     subprocess.run(["make", "-C", str(ROOT), "-f", "oracle/ref.mk", f"REF={REF}"], check=True,
@@ -163,6 +185,10 @@ def main():
         small_case(lib, "bunny_n32", 32, small_spec(6, 64, 48, seed=101), tmp)
         small_case(lib, "bunny_n40_halffov", 40, small_spec(6, 80, 64, seed=102, fov=0.5), tmp)
         runner_case(tmp)
+    # bunny_n40_halffov only for LolaOPT: its volume's shadow lies inside the
+    # detector, so LolaASM's pads (abs(Umax) - W, src/LolaASM.c:45-48) come out
+    # negative and its run ends in a segmentation fault
+    subprocess.run([sys.executable, __file__, "--asm-case", "bunny_n32"], check=True)
 
 
 if __name__ == "__main__":
