@@ -67,21 +67,24 @@ METRIC = "GUPS (1e9 voxel updates/s) N=512,1024: FP16-stored vs FP32 path, RMSE 
 #    20 packed + 2 reciprocals, i.e. 11 per voxel;
 # plus, per voxel and either way, its fetch: 2 index integer ops, 1 address,
 # the gathers (4 plain or 1 quad) and 4 widenings of 16-bit taps on the load
-# path, or 2 coordinate adds and 1 texture gather.  Mixed layouts fetch
+# path; 2 coordinate adds and 1 texture gather for the 2D texture layouts
+# (tex32, tex16); 1 index op and 1 texel fetch by index for the mixed layouts'
+# linear textures (LOLA_MIXED_TEX_LINEAR).  Mixed layouts fetch
 # MIXED_TEX_FRACTION of their voxels through the texture unit
-# (LOLA_MIXED_COLS_TEX_MASK = 0xABAB for f16qx, LOLA_MIXED_TEX_MASK = 0xAAAA
-# for f32qx, in lolacuda_internal.h).  The 16-bit quad
+# (LOLA_F16QX_TEX_MASK = 0xFFFF for f16qx: all of them; LOLA_MIXED_TEX_MASK =
+# 0xAAAA for f32qx, in lolacuda_internal.h).  The 16-bit quad
 # layouts store bilinear terms, so their interpolation is 3 FMAs instead of 6
 # operations (3 issue slots less per voxel, 1.5 on the paired path).  FP32
 # quads (f32q) are stored column by column and interpolated per voxel on the
 # paired path: 2 packed + 2 scalar instead of 3 packed per voxel (+1), in
 # exchange for the register moves the pairwise form needs (moves are not
 # counted for either form).
-MIXED_TEX_FRACTION = {"f16qx": 10 / 16, "f32qx": 0.5}  # LOLA_MIXED_(COLS_)TEX_MASK
+MIXED_TEX_FRACTION = {"f16qx": 1.0, "f32qx": 0.5}  # LOLA_F16QX_TEX_MASK, LOLA_MIXED_TEX_MASK
 _TERM_LAYOUTS = ("f16q", "bf16q", "f16qx")
 _COLUMN_LAYOUTS = ("f32q",)
 _LOAD_FETCH = {"f32": 7, "f16": 11, "bf16": 11, "f32q": 4, "f16q": 8, "bf16q": 8}
-_TEX_FETCH = 3
+_TEX_FETCH = 3         # 2D texture: two coordinate adds + the gather
+_TEX_LINEAR_FETCH = 2  # linear texture: the index op + the fetch
 
 
 def _fetch_cost(storage):
@@ -91,7 +94,7 @@ def _fetch_cost(storage):
     if storage in ("f16qx", "f32qx"):
         load = _LOAD_FETCH["f16q" if storage == "f16qx" else "f32q"]
         t = MIXED_TEX_FRACTION[storage]
-        return t * _TEX_FETCH + (1 - t) * load, 1 - t
+        return t * _TEX_LINEAR_FETCH + (1 - t) * load, 1 - t
     return _LOAD_FETCH[storage], 1.0
 
 
@@ -464,13 +467,22 @@ def roofline(args, lib, storage, st, probes, cfg=None) -> dict:
     if probes:
         ipu = instr_per_update(storage, ceil["paired_fraction"])
         issue = probes["issue_inst_per_s"] / ipu / 1e9
-        gather = probes["gather"][storage] / 1e9
+        # the gather pipes' own rate (an L1-resident image): an upper bound
+        # whatever the access pattern; the L2-resident random pattern beside it
+        gather = probes["gather_peak"][storage] / 1e9
+        gather_l2 = probes["gather"][storage] / 1e9
         bound, peak = ("issue", issue) if issue <= gather else ("gather", gather)
         ceil.update({"bound": bound, "peak": peak, "frac": achieved / peak,
                      "peak_issue": issue, "peak_gather": gather,
+                     "gather_l2_random": gather_l2, "frac_of_l2_random": achieved / gather_l2,
                      "instr_per_update": round(ipu, 2),
-                     "peak_source": "probe kernels on this GPU (lolaCudaProbeIssueRate / "
-                                    "lolaCudaProbeGatherRate)"})
+                     "peak_source": "probe kernels on this GPU (lolaCudaProbeIssueRate; "
+                                    "lolaCudaProbeGatherPeak: the layout's fetches inside an "
+                                    "L1-resident image; lolaCudaProbeGatherRate: at random "
+                                    "positions of an L2-resident projection)"})
+    pipes = pipe_utilisation(storage)
+    if pipes is not None:
+        ceil["ncu_pipes"] = pipes
     out["ceiling"] = ceil
     return out
 
@@ -491,6 +503,31 @@ def dram_traffic(storage, vpt, rows, batch, n):
         if (f[0], int(f[1]), int(f[2]), int(f[3]), int(f[4])) == (storage, vpt, rows, batch, n):
             return float(f[5]), f"ncu capture, {TRAFFIC_FILE.relative_to(ROOT)}"
     return None, None
+
+
+PIPES_FILE = ROOT / "profiles" / "passKernel_pipes.txt"
+
+
+def pipe_utilisation(storage):
+    """Hardware-pipe utilisation of the pass kernel for a storage layout, from
+    the committed ncu capture of a small case (lines `storage key=value ...`,
+    percentages of peak), or None."""
+    if not PIPES_FILE.exists():
+        return None
+    for line in PIPES_FILE.read_text().splitlines():
+        f = line.split()
+        if not f or line.startswith("#") or f[0] != storage:
+            continue
+        out = {}
+        for kv in f[1:]:
+            k, _, v = kv.partition("=")
+            try:
+                out[k] = float(v)
+            except ValueError:
+                out[k] = v
+        out["source"] = f"ncu capture, {PIPES_FILE.relative_to(ROOT)}"
+        return out
+    return None
 
 
 def time_e2e_slab(args, dist, scan, vs, o, storage) -> dict:
@@ -607,11 +644,12 @@ def run_gpu(args, rank, world, local):
 
     probes = None
     if not args.no_probes:
+        used = {args.storage, args.fp32_storage, args.fp32_quad_storage} - {"none"}
         probes = {"issue_inst_per_s": lib.lolaCudaProbeIssueRate(),
                   "gather": {s: lib.lolaCudaProbeGatherRate(STORAGE_IDS[s], scan.width,
-                                                            scan.height)
-                             for s in {args.storage, args.fp32_storage,
-                                       args.fp32_quad_storage} - {"none"}}}
+                                                            scan.height) for s in used},
+                  "gather_peak": {s: lib.lolaCudaProbeGatherPeak(STORAGE_IDS[s])
+                                  for s in used}}
 
     clocks = ClockSampler(0)
     head = time_device(args, dist, lib, scan, vs, o, d_images, args.storage, clocks)

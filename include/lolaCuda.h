@@ -451,8 +451,12 @@ int lolaCudaHostFree(void *h_ptr);
  * FP32 FMA issue rate of the current device, thread-instructions per second. */
 double lolaCudaProbeIssueRate(void);
 /* Voxel updates per second that the pass kernel's 2x2 gather pattern alone
- * sustains for a storage layout over a padded width x height detector. */
+ * sustains for a storage layout over a padded width x height detector, at
+ * random positions (L2-resident, no reuse in L1). */
 double lolaCudaProbeGatherRate(int storage, int width, int height);
+/* The same fetches inside an image small enough to stay in every SM's L1:
+ * the rate of the gather pipes themselves, an upper bound for any pattern. */
+double lolaCudaProbeGatherPeak(int storage);
 /* SM count, SM clock (kHz) and name of the current device. */
 int lolaCudaDeviceInfo(int *smCount, int *clockKHz, char *name, int nameLen);
 

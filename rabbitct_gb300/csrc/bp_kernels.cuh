@@ -383,6 +383,20 @@ __device__ __forceinline__ void texQuad(unsigned long long tex, float cx, float 
   p11 = q.w;
 }
 
+/* One texel of a mixed layout's quad texture by its integer pixel index in
+   the ring slot (LOLA_MIXED_TEX_LINEAR: a linear texture over the slot), in
+   the order texQuad gives. */
+template <bool COLS, bool RAW = false>
+__device__ __forceinline__ void texQuadLinear(unsigned long long tex, uint32_t idx, float &p00,
+    float &p10, float &p01, float &p11)
+{
+  const float4 q = tex1Dfetch<float4>((cudaTextureObject_t)tex, (int)idx);
+  p00 = q.x;
+  p10 = (COLS && !RAW) ? q.z : q.y;
+  p01 = (COLS && !RAW) ? q.y : q.z;
+  p11 = q.w;
+}
+
 /* ---- packing: FP32 detector image -> zero-padded stored layout ------------- */
 
 struct PackArgs {
@@ -498,9 +512,15 @@ __device__ __forceinline__ void applyProjection(const TileProj &tp, const void *
       const float off = (float)a.margin + 1.0f;
       texTaps(tex, tx + off, ty + off, p00, p10, p01, p11);
     } else if (Layout<S>::kMixed && ((TEXMASK >> k) & 1u)) {
-      /* point fetch of texel (tx + M, ty + M): any coordinate inside it works */
-      const float off = (float)a.margin + 0.5f;
-      texQuad<Layout<S>::kCols>(tex, tx + off, ty + off, p00, p10, p01, p11);
+      if (LOLA_MIXED_TEX_LINEAR) {
+        /* the texel at the load path's index; any index past the slot reads 0 */
+        const uint32_t idx = __float_as_uint(fmaf(ty, pitchF, tx + biasF)) - 0x4B000000u;
+        texQuadLinear<Layout<S>::kCols>(tex, idx, p00, p10, p01, p11);
+      } else {
+        /* point fetch of texel (tx + M, ty + M): any coordinate inside it works */
+        const float off = (float)a.margin + 0.5f;
+        texQuad<Layout<S>::kCols>(tex, tx + off, ty + off, p00, p10, p01, p11);
+      }
     } else {
       uint32_t idx = __float_as_uint(fmaf(ty, pitchF, tx + biasF)) - 0x4B000000u;
       idx = min(idx, maxIdx);  /* memory-safety net; never active on valid input */
@@ -641,9 +661,9 @@ __device__ __forceinline__ void pairedUpdate(const TileProj &tp, float fi, float
 
 /* Texture mask of a mixed layout in the pass kernel. */
 template <int S> struct PassTexMask {
-  static constexpr unsigned kValue = !Layout<S>::kCols ? LOLA_MIXED_TEX_MASK
-                                     : S == LOLA_STORE_F32QX ? LOLA_F32QX_COLS_TEX_MASK
-                                                             : LOLA_MIXED_COLS_TEX_MASK;
+  static constexpr unsigned kValue = S == LOLA_STORE_F16QX ? LOLA_F16QX_TEX_MASK
+                                     : !Layout<S>::kCols   ? LOLA_MIXED_TEX_MASK
+                                                           : LOLA_F32QX_COLS_TEX_MASK;
 };
 
 /* The paired update on the stored ring (loads, texture or both).  Voxels
@@ -681,10 +701,18 @@ __device__ __forceinline__ void applyPairs(const TileProj &tp, const void *img,
       texTaps(tex, tcx - nqx, tcy - nqy, p00, p10, p01, p11);
     } else {
       if (Layout<S>::kMixed && ((TEXMASK >> k) & 1u)) {
-        if ((COLSMASK >> k) & 1u)
+        if (LOLA_MIXED_TEX_LINEAR) {
+          /* an index past the slot reads 0: no clamp needed for memory safety */
+          const uint32_t idx = __float_as_uint(idxf) - 0x4B000000u;
+          if ((COLSMASK >> k) & 1u)
+            texQuadLinear<Layout<S>::kCols, true>(tex, idx, p00, p10, p01, p11);
+          else
+            texQuadLinear<Layout<S>::kCols>(tex, idx, p00, p10, p01, p11);
+        } else if ((COLSMASK >> k) & 1u) {
           texQuad<Layout<S>::kCols, true>(tex, tcx - nqx, tcy - nqy, p00, p10, p01, p11);
-        else
+        } else {
           texQuad<Layout<S>::kCols>(tex, tcx - nqx, tcy - nqy, p00, p10, p01, p11);
+        }
       } else {
         uint32_t idx = __float_as_uint(idxf) - 0x4B000000u;
         idx = min(idx, maxIdx);  /* memory-safety net; never active on valid input */
@@ -856,7 +884,10 @@ __device__ __forceinline__ void setupTile(const LolaPassParams &P, const PassArg
 template <int S, int VPT, int ROWS> struct MinBlocks {
   static constexpr bool kWide32 = S == LOLA_STORE_F32 || S == LOLA_STORE_F32Q ||
                                   S == LOLA_STORE_TEX32 || S == LOLA_STORE_F32QX;
-  static constexpr int kWarps = (VPT <= 8) ? 40 : (kWide32 ? 36 : 28);
+  /* f16qx with every voxel by texture widens nothing itself: 32 warps (64
+     registers) measured 1781 vs 1767 GUPS at 28 and 1668 at 24 */
+  static constexpr bool kAllTex = S == LOLA_STORE_F16QX && LOLA_F16QX_TEX_MASK == 0xFFFFu;
+  static constexpr int kWarps = (VPT <= 8) ? 40 : (kWide32 ? 36 : (kAllTex ? 32 : 28));
   static constexpr int kValue = kWarps / ROWS;
 };
 #ifdef LOLA_MIN_BLOCKS
@@ -983,15 +1014,6 @@ int launchPassShape(const PassArgs &a, const LolaPassParams *P, cudaStream_t str
   constexpr int TX = LOLA_WARP_X, TY = 32 * ROWS / TX;
   const dim3 grid((N + TX - 1) / TX, (N + TY - 1) / TY, (nz + VPT - 1) / VPT);
   (void)cudaGetLastError();
-  if constexpr (Layout<S>::kMixed && Layout<S>::kCols && VPT == 16 && ROWS == 4 &&
-                PassTexMask<S>::kValue != LOLA_MIXED_TEX_MASK) {
-    /* small volumes (N <= LOLA_COLS_MASK_MIN_N, coarse voxels) read fewer
-       voxels through the texture unit */
-    if (N <= LOLA_COLS_MASK_MIN_N) {
-      passKernel<S, VPT, ROWS, KAHAN, LOLA_MIXED_TEX_MASK><<<grid, block, 0, stream>>>(a, *P);
-      return (int)cudaGetLastError();
-    }
-  }
   passKernel<S, VPT, ROWS, KAHAN><<<grid, block, 0, stream>>>(a, *P);
   return (int)cudaGetLastError();
 }

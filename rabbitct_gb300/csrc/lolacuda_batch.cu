@@ -340,14 +340,24 @@ int build(LolaCudaBatch *bt, const LolaCudaJob *jobs)
       for (int s = 0; s < b; ++s) {
         cudaResourceDesc rd;
         memset(&rd, 0, sizeof(rd));
-        rd.resType = cudaResourceTypePitch2D;
-        rd.res.pitch2D.devPtr = bt->d_ring + ringOffset[j] + (size_t)s * hj[j].slotBytes;
+        unsigned char *slotBase = bt->d_ring + ringOffset[j] + (size_t)s * hj[j].slotBytes;
         const int bits = 8 * pix / ch;
-        rd.res.pitch2D.desc = cudaCreateChannelDesc(bits, ch > 1 ? bits : 0, ch > 1 ? bits : 0,
-            ch > 1 ? bits : 0, cudaChannelFormatKindFloat);
-        rd.res.pitch2D.width = (size_t)hj[j].pitch;
-        rd.res.pitch2D.height = (size_t)hj[j].rows;
-        rd.res.pitch2D.pitchInBytes = (size_t)hj[j].pitch * pix;
+        const cudaChannelFormatDesc texel = cudaCreateChannelDesc(bits, ch > 1 ? bits : 0,
+            ch > 1 ? bits : 0, ch > 1 ? bits : 0, cudaChannelFormatKindFloat);
+        if (LOLA_MIXED_TEX_LINEAR && ch == 4) {
+          /* mixed layouts: quads fetched by their integer index in the slot */
+          rd.resType = cudaResourceTypeLinear;
+          rd.res.linear.devPtr = slotBase;
+          rd.res.linear.desc = texel;
+          rd.res.linear.sizeInBytes = hj[j].slotBytes;
+        } else {
+          rd.resType = cudaResourceTypePitch2D;
+          rd.res.pitch2D.devPtr = slotBase;
+          rd.res.pitch2D.desc = texel;
+          rd.res.pitch2D.width = (size_t)hj[j].pitch;
+          rd.res.pitch2D.height = (size_t)hj[j].rows;
+          rd.res.pitch2D.pitchInBytes = (size_t)hj[j].pitch * pix;
+        }
         cudaTextureDesc td;
         memset(&td, 0, sizeof(td));
         td.addressMode[0] = cudaAddressModeBorder;

@@ -373,16 +373,26 @@ static int planInit(LolaCudaPlan *p)
     for (int i = 0; i < p->ringSlots; i++) {
       struct cudaResourceDesc rd;
       memset(&rd, 0, sizeof(rd));
-      rd.resType = cudaResourceTypePitch2D;
-      rd.res.pitch2D.devPtr = (char *)p->d_ring + (size_t)i * s->slotElems * s->elemBytes;
       const int ch = texChannels(s->storage);
       const int bits = 8 * s->elemBytes / ch;
-      rd.res.pitch2D.desc = cudaCreateChannelDesc(bits, ch > 1 ? bits : 0, ch > 1 ? bits : 0,
-          ch > 1 ? bits : 0, cudaChannelFormatKindFloat);
-      rd.res.pitch2D.width = (size_t)s->pitch;
-      rd.res.pitch2D.height = (size_t)s->rows;
-      rd.res.pitch2D.pitchInBytes = (size_t)s->pitch * s->elemBytes;
-      if (LOLA_TEX_ARRAYS) {
+      const struct cudaChannelFormatDesc texel = cudaCreateChannelDesc(bits,
+          ch > 1 ? bits : 0, ch > 1 ? bits : 0, ch > 1 ? bits : 0, cudaChannelFormatKindFloat);
+      void *slotBase = (char *)p->d_ring + (size_t)i * s->slotElems * s->elemBytes;
+      if (LOLA_MIXED_TEX_LINEAR && ch == 4) {
+        /* mixed layouts: quads fetched by their integer index in the slot */
+        rd.resType = cudaResourceTypeLinear;
+        rd.res.linear.devPtr = slotBase;
+        rd.res.linear.desc = texel;
+        rd.res.linear.sizeInBytes = s->slotElems * (size_t)s->elemBytes;
+      } else {
+        rd.resType = cudaResourceTypePitch2D;
+        rd.res.pitch2D.devPtr = slotBase;
+        rd.res.pitch2D.desc = texel;
+        rd.res.pitch2D.width = (size_t)s->pitch;
+        rd.res.pitch2D.height = (size_t)s->rows;
+        rd.res.pitch2D.pitchInBytes = (size_t)s->pitch * s->elemBytes;
+      }
+      if (LOLA_TEX_ARRAYS && rd.resType == cudaResourceTypePitch2D) {
         /* a CUDA array per slot (block-linear), written through a surface */
         const struct cudaChannelFormatDesc cd = rd.res.pitch2D.desc;
         CUDA_TRY(cudaMallocArray(&p->texArrays[i], &cd, (size_t)s->pitch, (size_t)s->rows,

@@ -102,25 +102,30 @@ typedef struct {
 #endif
 
 /* 1: f16qx stores its quads column by column.  A texel then lands as the two
- * column pairs that one packed FMA interpolates in x, so pairs read wholly
- * through the texture unit need no register moves, and the pass kernel uses
- * LOLA_MIXED_COLS_TEX_MASK: 10 of every 16 voxels by texture, one whole pair
- * and three half pairs in each 8.  Measured on GB300 at N=1024 (f16qx GUPS):
- * 1514-1518 vs 1468-1470 for the row order with 0xAAAA; with the column
- * order 0x3B3B 1481, 0x2F2F 1463, 0x3F3F 1442, 0x0F0F 1399, 0xFFFF 1302; with
- * the row order 0xABAB 1489-1491, 0xBABA 1485, 0xBBBB 1452, 0xFFFF 1297. */
+ * column pairs that one packed FMA interpolates in x, so voxel pairs read
+ * wholly through the texture unit need no register moves. */
 #ifndef LOLA_F16QX_COLS
 #define LOLA_F16QX_COLS 1
 #endif
-#ifndef LOLA_MIXED_COLS_TEX_MASK
-#define LOLA_MIXED_COLS_TEX_MASK 0xABABu
+/* f16qx: the voxels (bit k of a thread's column) that fetch through the
+ * texture unit; the others load.  With linear textures (LOLA_MIXED_TEX_LINEAR)
+ * every voxel by texture measured fastest on GB300 at N=1024 (f16qx GUPS,
+ * batch 16, 16 x 4 tiles, one box): 0xFFFF 1757-1767, 0xBBBB 1675,
+ * 0xBFBF 1672, 0xEEEE 1658, 0xFBFB 1633, 0xABAB 1619-1625 — and 2D textures
+ * at float coordinates with 0xABAB, the earlier default, 1544.  At N=512 all
+ * by texture 1438 against 1297 for the earlier default. */
+#ifndef LOLA_F16QX_TEX_MASK
+#define LOLA_F16QX_TEX_MASK 0xFFFFu
 #endif
-/* Volumes up to this edge (coarser voxels: each spans more detector pixels)
- * run the column-ordered mixed layouts with LOLA_MIXED_TEX_MASK instead, on
- * the default 16 x 4 tiles: at N=512 f16qx measured 1.8 % faster that way,
- * and the 64-job batch of N = 128..384 volumes 4.6 % (940 vs 899 GUPS). */
-#ifndef LOLA_COLS_MASK_MIN_N
-#define LOLA_COLS_MASK_MIN_N 512
+
+/* 1: the mixed layouts' texture voxels fetch their quad with tex1Dfetch from
+ * a linear texture over the ring slot, by the same integer pixel index the
+ * load path forms: no float texture coordinates (two FADDs per voxel fewer)
+ * and an index past the slot reads zero.  0: tex2D point fetch from a
+ * pitch-linear 2D texture at float coordinates.  Measured on GB300 at
+ * N=1024 with the mask 0xABAB: f16qx 1625 vs 1544 GUPS. */
+#ifndef LOLA_MIXED_TEX_LINEAR
+#define LOLA_MIXED_TEX_LINEAR 1
 #endif
 
 /* 1: f32qx stores its quads column by column and the pass kernel uses

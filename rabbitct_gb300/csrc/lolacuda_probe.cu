@@ -6,9 +6,13 @@
  *          update) bounds its update rate.
  *  gather  the pass kernel's local 2D gather pattern with trivial arithmetic:
  *          each warp reads, for 32 lanes at detector columns spaced 1.25 px
- *          apart, the 2x2 taps of an L2-resident stored projection, in the
- *          kernel's storage layouts (4 x 4 B, 4 x 2 B, 1 x 16 B or 1 x 8 B per
- *          update).  Returns updates / s the gather path alone sustains.
+ *          apart, the 2x2 taps of a stored projection, in the kernel's storage
+ *          layouts (4 x 4 B, 4 x 2 B, 1 x 16 B or 1 x 8 B per update, or one
+ *          texel fetch).  Returns updates / s the gather path alone sustains:
+ *          lolaCudaProbeGatherRate at random positions of a full-size,
+ *          L2-resident projection (no reuse in L1), lolaCudaProbeGatherPeak
+ *          inside a small image that every SM keeps in L1 — the rate of the
+ *          gather pipes themselves, an upper bound for any access pattern.
  * Both run on every SM with enough warps to saturate it and are timed with
  * CUDA events on the caller's stream.
  */
@@ -44,7 +48,8 @@ __global__ void __launch_bounds__(256) issueProbe(float *out, int iters, float a
 }
 
 /* kind: 0 = 4 x FP32 taps, 1 = 4 x 16-bit taps, 2 = 1 x 16 B quad, 3 = 1 x 8 B quad,
- * 4 = one 4-texel texture gather (tld4), 5 = one point fetch of an RGBA texel */
+ * 4 = one 4-texel texture gather (tld4), 5 = one point fetch of an RGBA texel,
+ * 6 = one fetch of an RGBA texel by integer index from a linear texture */
 template <int KIND>
 __global__ void __launch_bounds__(256) gatherProbe(const void *img, int pitch, int rows,
     int iters, float *out, cudaTextureObject_t tex)
@@ -77,10 +82,13 @@ __global__ void __launch_bounds__(256) gatherProbe(const void *img, int pitch, i
       const float cy = (float)(idx / (uint32_t)pitch) + 1.0f;
       const float4 g = tex2Dgather<float4>(tex, cx, cy, 0);
       acc += (g.x + g.y) + (g.z + g.w);
-    } else {
+    } else if (KIND == 5) {
       const float cx = (float)(idx % (uint32_t)pitch) + 0.5f;
       const float cy = (float)(idx / (uint32_t)pitch) + 0.5f;
       const float4 g = tex2D<float4>(tex, cx, cy);
+      acc += (g.x + g.y) + (g.z + g.w);
+    } else {
+      const float4 g = tex1Dfetch<float4>(tex, (int)idx);
       acc += (g.x + g.y) + (g.z + g.w);
     }
   }
@@ -128,19 +136,35 @@ extern "C" double lolaCudaProbeIssueRate(void)
 /* Voxel updates per second the gather alone sustains, for a storage layout
  * (LOLA_STORE_*) over a width x height detector padded like the pass kernel. */
 static double probeKind(int kind, int elem, int channels, int width, int height);
+static double probeStorage(int storage, int width, int height);
 
 extern "C" double lolaCudaProbeGatherRate(int storage, int width, int height)
+{
+  return probeStorage(storage, width, height);
+}
+
+/* The same fetches inside a 112 x 16 image (28 KB of FP32 quads) that stays
+ * in every SM's L1: the gather pipes' own rate.  (gatherProbe draws bases in
+ * the first (pitch - 64) x (rows - 2) pixels, so with 64 + 48 columns every
+ * fetch stays inside the image.) */
+extern "C" double lolaCudaProbeGatherPeak(int storage)
+{
+  return probeStorage(storage, -112, -16);
+}
+
+static double probeStorage(int storage, int width, int height)
 {
   if (storage == LOLA_STORE_F16QX || storage == LOLA_STORE_F32QX) {
     /* the two pipes run in parallel on their shares of the voxels */
     const int elem = storage == LOLA_STORE_F16QX ? 8 : 16;
-    const double lsu = probeKind(elem == 8 ? 3 : 2, elem, 1, width, height);
-    const double tex = probeKind(5, elem, 4, width, height);
-    /* the pass kernel's texture share (PassTexMask in bp_kernels.cuh; the
-       share of volumes above LOLA_COLS_MASK_MIN_N) */
+    /* the pass kernel's texture share (PassTexMask in bp_kernels.cuh) */
     const unsigned mask = storage == LOLA_STORE_F16QX
-                              ? (LOLA_F16QX_COLS ? LOLA_MIXED_COLS_TEX_MASK : LOLA_MIXED_TEX_MASK)
+                              ? LOLA_F16QX_TEX_MASK
                               : (LOLA_F32QX_COLS ? LOLA_F32QX_COLS_TEX_MASK : LOLA_MIXED_TEX_MASK);
+    const double lsu = (mask & 0xFFFFu) == 0xFFFFu
+                           ? 1.0
+                           : probeKind(elem == 8 ? 3 : 2, elem, 1, width, height);
+    const double tex = probeKind(LOLA_MIXED_TEX_LINEAR ? 6 : 5, elem, 4, width, height);
     const double ft = __builtin_popcount(mask & 0xFFFFu) / 16.0;
     if (lsu <= 0.0 || tex <= 0.0)
       return -1.0;
@@ -166,9 +190,11 @@ extern "C" double lolaCudaProbeGatherRate(int storage, int width, int height)
   return probeKind(kind, elem, 1, width, height);
 }
 
+/* width, height < 0: an unpadded |width| x |height| image (L1 resident) */
 static double probeKind(int kind, int elem, int channels, int width, int height)
 {
-  const int pitch = (width + 128 + 31) & ~31, rows = height + 128;
+  const int pitch = width < 0 ? -width : (width + 128 + 31) & ~31;
+  const int rows = height < 0 ? -height : height + 128;
   const size_t bytes = (size_t)pitch * rows * elem;
   void *img = nullptr;
   float *out = nullptr;
@@ -182,14 +208,22 @@ static double probeKind(int kind, int elem, int channels, int width, int height)
   cudaTextureObject_t tex = 0;
   if (kind >= 4) {
     cudaResourceDesc rd = {};
-    rd.resType = cudaResourceTypePitch2D;
-    rd.res.pitch2D.devPtr = img;
     const int bits = 8 * elem / channels;
-    rd.res.pitch2D.desc = cudaCreateChannelDesc(bits, channels > 1 ? bits : 0,
+    const cudaChannelFormatDesc texel = cudaCreateChannelDesc(bits, channels > 1 ? bits : 0,
         channels > 1 ? bits : 0, channels > 1 ? bits : 0, cudaChannelFormatKindFloat);
-    rd.res.pitch2D.width = (size_t)pitch;
-    rd.res.pitch2D.height = (size_t)rows;
-    rd.res.pitch2D.pitchInBytes = (size_t)pitch * elem;
+    if (kind == 6) {
+      rd.resType = cudaResourceTypeLinear;
+      rd.res.linear.devPtr = img;
+      rd.res.linear.desc = texel;
+      rd.res.linear.sizeInBytes = bytes;
+    } else {
+      rd.resType = cudaResourceTypePitch2D;
+      rd.res.pitch2D.devPtr = img;
+      rd.res.pitch2D.desc = texel;
+      rd.res.pitch2D.width = (size_t)pitch;
+      rd.res.pitch2D.height = (size_t)rows;
+      rd.res.pitch2D.pitchInBytes = (size_t)pitch * elem;
+    }
     cudaTextureDesc td = {};
     td.addressMode[0] = td.addressMode[1] = cudaAddressModeBorder;
     td.filterMode = cudaFilterModePoint;
@@ -212,7 +246,8 @@ static double probeKind(int kind, int elem, int channels, int width, int height)
     case 2: gatherProbe<2><<<blocks, threads>>>(img, pitch, rows, it, out, tex); break;
     case 3: gatherProbe<3><<<blocks, threads>>>(img, pitch, rows, it, out, tex); break;
     case 4: gatherProbe<4><<<blocks, threads>>>(img, pitch, rows, it, out, tex); break;
-    default: gatherProbe<5><<<blocks, threads>>>(img, pitch, rows, it, out, tex); break;
+    case 5: gatherProbe<5><<<blocks, threads>>>(img, pitch, rows, it, out, tex); break;
+    default: gatherProbe<6><<<blocks, threads>>>(img, pitch, rows, it, out, tex); break;
     }
   };
   launch(64);

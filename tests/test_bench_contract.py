@@ -44,7 +44,8 @@ def test_roofline_shape(bench):
     st = types.SimpleNamespace(tilePassesFast=378_000, tilePassesSlow=0,
                                tilePassesSkipped=147_000, tilePassesPaired=365_000,
                                passes=1, passMs=12.0)
-    probes = {"issue_inst_per_s": 3.9e13, "gather": {"f16qx": 1.8e12}}
+    probes = {"issue_inst_per_s": 3.9e13, "gather": {"f16qx": 1.8e12},
+              "gather_peak": {"f16qx": 2.6e12}}
     r = bench.roofline(a, None, "f16qx", st, probes)
     assert r["bound"] == "hbm" and r["unit"] == "GB/s"
     peaks = ROOT / "MEASURED_PEAKS.json"
@@ -59,6 +60,7 @@ def test_roofline_shape(bench):
     c = r["ceiling"]
     assert c["unit"] == "Gupdate/s" and c["bound"] in ("gather", "issue")
     assert c["peak"] == pytest.approx(min(c["peak_gather"], c["peak_issue"]))
+    assert c["peak_gather"] >= c["gather_l2_random"]
     assert 0 < c["paired_fraction"] <= 1
 
 
