@@ -567,6 +567,26 @@ def time_e2e_slab(args, dist, scan, vs, o, storage) -> dict:
             "path": "plan API per z-slab, pinned host"}
 
 
+def host_link_gbs(lib, h_buf, nbytes) -> dict:
+    """Pinned host <-> device copy bandwidth of this machine (GB/s), median of 3
+    synchronous copies of `nbytes` each way: the e2e figure moves 6.7 GB in and
+    4.3 GB out per step, and the host link is shared with other tenants."""
+    d = lib.lolaCudaDeviceAlloc(nbytes)
+    if not d:
+        return None
+    out = {}
+    for name, fn, args_ in (("h2d", lib.lolaCudaCopyToDevice, (d, h_buf, nbytes)),
+                            ("d2h", lib.lolaCudaCopyToHost, (h_buf, d, nbytes))):
+        ts = []
+        for _ in range(3):
+            t0 = time.perf_counter()
+            fn(*args_)
+            ts.append(time.perf_counter() - t0)
+        out[name] = nbytes / statistics.median(ts) / 1e9
+    lib.lolaCudaDeviceFree(d)
+    return out
+
+
 def time_e2e(args, dist, scan, vs, o, storage) -> dict:
     """Module API (prepare / backprojection per projection / finish) with
     pinned host buffers, as rabbitRunner drives a module with -b 1 -a."""
@@ -596,6 +616,7 @@ def time_e2e(args, dist, scan, vs, o, storage) -> dict:
                                        voxels_per_thread=args.vpt, rows_per_block=args.rows,
                                        exit_on_error=0, staging=args.staging,
                                        sync_each_call=0)), "config")
+    link = host_link_gbs(lib, hv, min(nbytes_vol, 1 << 30))
     times, phases = [], []
     for step in range(1 + args.e2e_steps):
         vol.fill(0.0)  # the runner hands over a zeroed volume (src/rabbitRunner.c:192)
@@ -624,6 +645,7 @@ def time_e2e(args, dist, scan, vs, o, storage) -> dict:
                     "host, syncEachCall 0; volume upload and download overlapped with the first "
                     "and last pass",
             "checksum_mid_slice": checksum,
+            "host_link_gbs": link,
             "phases_ms": {"prepare": 1e3 * statistics.median(p[0] for p in phases),
                           "calls": 1e3 * statistics.median(p[1] for p in phases),
                           "finish": 1e3 * statistics.median(p[2] for p in phases)}}
