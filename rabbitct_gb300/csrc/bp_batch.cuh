@@ -7,7 +7,7 @@
  * work items — (job, tile) pairs, numbered job by job — from an atomic
  * counter until the wave is done, so small and large jobs balance across the
  * SMs without one launch per job.  A work item is exactly a passKernel tile
- * of 8 rows of 8 voxels per thread (LOLA_WARP_X x 256 / LOLA_WARP_X x 8
+ * of LOLA_BATCH_ROWS warps and LOLA_BATCH_VPT voxels per thread (8 x 16 x 16
  * voxels, in registers across the wave's projections).  The host
  * captures the whole sequence of waves into a CUDA graph once and replays it.
  */
@@ -59,21 +59,28 @@ __global__ void __launch_bounds__(256) batchPackKernel(const LolaBatchWave w)
 #define LOLA_BATCH_PAIRED 1
 #endif
 
-/* Mixed layouts in the batched pass fetch every quad through loads: with
-   texture fetches in flight its per-item state no longer fits 64 registers
-   (1.4 KB of spills at the passKernel mask).  Same values either way. */
+/* Mixed layouts in the batched pass fetch every quad through loads.  The
+   texture object of a work item's projection comes from device memory (the
+   wave's per-job handle table), not from the kernel parameters as in
+   passKernel, and a texture fetch through such a handle kept f16qx's
+   per-item state far beyond its registers (6 KB of spills).  Same values
+   either way: the FP16 point fetch widens exactly. */
 #ifndef LOLA_BATCH_TEX_MASK
 #define LOLA_BATCH_TEX_MASK 0u
 #endif
 
+/* resident blocks of LOLA_BATCH_ROWS warps per SM: passKernel's occupancy
+   for a load path (36 warps for FP32 layouts, 28 for 16-bit ones) */
 #ifndef LOLA_BATCH_MIN_BLOCKS
-#define LOLA_BATCH_MIN_BLOCKS 4
+#define LOLA_BATCH_MIN_BLOCKS(S)                                                            \
+  ((MinBlocks<S, LOLA_BATCH_VPT, LOLA_BATCH_ROWS>::kWide32 ? 36 : 28) / LOLA_BATCH_ROWS)
 #endif
 
 template <int S, bool KAHAN>
-__global__ void __launch_bounds__(256, LOLA_BATCH_MIN_BLOCKS) batchPassKernel(const LolaBatchWave w)
+__global__ void __launch_bounds__(32 * LOLA_BATCH_ROWS, LOLA_BATCH_MIN_BLOCKS(S))
+    batchPassKernel(const LolaBatchWave w)
 {
-  constexpr int VPT = 8, ROWS = 8;
+  constexpr int VPT = LOLA_BATCH_VPT, ROWS = LOLA_BATCH_ROWS;
   constexpr int TX = LOLA_WARP_X, TY = 32 * ROWS / TX;
   __shared__ TileProj sp[LOLA_MAX_BATCH];
   /* the current work item: its job's descriptor and tile, shared by the
@@ -188,7 +195,7 @@ int launchBatchPack(const LolaBatchWave *w, cudaStream_t stream)
 template <int S>
 int launchBatchPass(const LolaBatchWave *w, int blocks, cudaStream_t stream)
 {
-  const dim3 block(32, 8);
+  const dim3 block(32, LOLA_BATCH_ROWS);
   (void)cudaGetLastError();  /* report this launch's error, not an earlier one */
   if (w->accumulation == LOLA_ACCUM_KAHAN)
     batchPassKernel<S, true><<<blocks, block, 0, stream>>>(*w);
@@ -202,9 +209,9 @@ int batchOccupancy(int accumulation, int *blocks)
 {
   cudaError_t e = accumulation == LOLA_ACCUM_KAHAN
                       ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                            blocks, batchPassKernel<S, true>, 256, 0)
+                            blocks, batchPassKernel<S, true>, 32 * LOLA_BATCH_ROWS, 0)
                       : cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                            blocks, batchPassKernel<S, false>, 256, 0);
+                            blocks, batchPassKernel<S, false>, 32 * LOLA_BATCH_ROWS, 0);
   return (int)e;
 }
 

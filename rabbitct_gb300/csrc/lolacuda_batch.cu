@@ -313,10 +313,13 @@ int build(LolaCudaBatch *bt, const LolaCudaJob *jobs)
     J.slotBytes = J.slotElems * pix;
     J.voxelSize = g.voxelSize;
     J.originIndex = g.originIndex;
-    /* the persistent pass's tiles: LOLA_WARP_X x (256 / LOLA_WARP_X) x 8 */
-    J.tilesX = (J.N + LOLA_WARP_X - 1) / LOLA_WARP_X;
-    J.tilesY = (J.N + 256 / LOLA_WARP_X - 1) / (256 / LOLA_WARP_X);
-    J.tilesZ = (J.N + 7) / 8;
+    /* the persistent pass's work items (LOLA_BATCH_VPT, LOLA_BATCH_ROWS) */
+    {
+      const int ty = 32 * LOLA_BATCH_ROWS / LOLA_WARP_X;
+      J.tilesX = (J.N + LOLA_WARP_X - 1) / LOLA_WARP_X;
+      J.tilesY = (J.N + ty - 1) / ty;
+      J.tilesZ = (J.N + LOLA_BATCH_VPT - 1) / LOLA_BATCH_VPT;
+    }
     J.nproj = jobs[j].projections;
     J.volume = jobs[j].d_volume;
     J.images = jobs[j].d_images;

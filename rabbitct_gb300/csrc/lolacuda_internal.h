@@ -163,6 +163,12 @@ typedef struct {
   int *d_error;           /* device flag set on a wait timeout */
 } LolaStageDesc;
 
+/* Work item of the persistent batched pass (bp_batch.cuh): a passKernel tile
+ * of LOLA_BATCH_ROWS warps, LOLA_WARP_X x (32 LOLA_BATCH_ROWS / LOLA_WARP_X) x
+ * LOLA_BATCH_VPT voxels (the default pass tile, 8 x 16 x 16). */
+#define LOLA_BATCH_VPT 16
+#define LOLA_BATCH_ROWS 4
+
 /* One reconstruction of a batch (bp_batch.cuh), as the device sees it. */
 typedef struct {
   float *volume;                    /* N^3 FP32 */

@@ -246,6 +246,7 @@ extern "C" int lolaCudaBackprojectNoAlloc(const LolaCudaGeometry *g, const LolaC
     return 0;
 
   LolaPassParams P;
+  memset(&P, 0, sizeof(P));  /* no tile counters; every field set below or zero */
   for (int done = 0; done < count;) {
     const int n = (count - done < perPass) ? count - done : perPass;
     int rc = lolaLaunchPack(&st, d_images + (size_t)done * imageStride, imageStride, ring, 0, n,

@@ -44,10 +44,10 @@ def test_batch_matches_plans_and_oracle(scans, storage, mode):
         jobs.append(dict(n=n, voxel_size=vs, origin_index=o, width=scan.width,
                          height=scan.height, d_images=d_img.ptr, matrices=scan.matrices,
                          d_volume=d_vol.ptr))
-    # the persistent pass computes 8 x 8 tiles; the branches and the plans use
-    # the same shape so every voxel sees the same tile origin
+    # the persistent pass computes the default 16 x 4 tiles; the branches and
+    # the plans use the same shape so every voxel sees the same tile origin
     with Batch(jobs, storage=storage, batch=4, batch_mode=mode, batch_branches=3,
-               batch_tune=0, voxels_per_thread=8, rows_per_block=8) as bt:
+               batch_tune=0, voxels_per_thread=16, rows_per_block=4) as bt:
         info = bt.info()
         waves = [-(-p // 4) for _, _, _, p, _ in JOBS]
         assert info.jobs == len(JOBS) and info.waves == max(waves)
@@ -60,7 +60,7 @@ def test_batch_matches_plans_and_oracle(scans, storage, mode):
         second = [v.to_array((n, n, n), np.float32) for (_, v), (n, *_rest) in zip(bufs, scans)]
     for (n, vs, o, scan), got, again in zip(scans, first, second):
         with Plan(n, vs, o, scan.width, scan.height, storage=storage, batch=4,
-                  voxels_per_thread=8, rows_per_block=8) as plan:
+                  voxels_per_thread=16, rows_per_block=4) as plan:
             plan.backproject_host(scan.images, scan.matrices)
             want = plan.download()
         assert np.array_equal(got, want), (n, storage)
