@@ -11,7 +11,7 @@ Lines printed (rank 0, one JSON object):
   value   device-resident throughput of the FP16-stored path (projections
           already in HBM when the timed region starts; CUDA events on the
           plan's stream); tile shape, batch and staging are picked by the
-          autotuner on the first 32 projections before the timed region
+          autotuner on the first 64 projections before the timed region
   fp32_path, fp32_quads  the plain FP32 path (four FP32 taps per update) and
           FP32 storage as 2x2 quads (the same results), measured the same way
   e2e     the same metric through the RabbitCT module API (prepare, one
@@ -140,7 +140,7 @@ def parse_args():
     ap.add_argument("--rows", type=int, default=4)
     ap.add_argument("--autotune", type=int, default=1,
                     help="1: pick tile shape / batch / staging with lolaCudaAutotune on the "
-                         "first 32 projections before timing (untimed)")
+                         "first 64 projections before timing (untimed)")
     ap.add_argument("--staging", type=int, default=None,
                     help="1/0: force shared-memory staging on/off (default: library default)")
     ap.add_argument("--e2e-steps", type=int, default=4)
@@ -384,7 +384,7 @@ def total_updates(args, scan, dist) -> float:
 
 
 def tuned_config(args, dist, scan, vs, o, d_images, storage):
-    """The configuration a run uses: autotuned on the first 32 projections
+    """The configuration a run uses: autotuned on the first 64 projections
     (untimed) or taken from the command line."""
     from rabbitct_gb300.lolacuda import autotune, config
     base = config(storage=storage, batch=args.batch, voxels_per_thread=args.vpt,
@@ -392,7 +392,7 @@ def tuned_config(args, dist, scan, vs, o, d_images, storage):
     if not args.autotune:
         return base, None
     cfg, tried = autotune(args.n, vs, o, scan.width, scan.height, d_images.ptr,
-                          scan.matrices[:32], cfg=base, slab=my_slab(args, dist))
+                          scan.matrices[:64], cfg=base, slab=my_slab(args, dist))
     return cfg, tried
 
 

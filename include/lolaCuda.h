@@ -84,7 +84,7 @@ int lolaCudaBackprojection(RabbitCtGlobalData *data);
 int lolaCudaFinish(RabbitCtGlobalData *data);
 
 /* ---- 2. Configuration ------------------------------------------------------ */
-#define LOLA_MAX_BATCH 32
+#define LOLA_MAX_BATCH 64
 
 enum {
   LOLA_STORE_F32 = 0,   /* 4 FP32 taps per update */

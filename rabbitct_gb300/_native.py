@@ -123,7 +123,7 @@ class LolaCudaStats(C.Structure):
 STORAGE = {"f32": 0, "f16": 1, "bf16": 2, "f32q": 3, "f16q": 4, "bf16q": 5, "tex32": 6,
            "tex16": 7, "f16qx": 8, "f32qx": 9}
 ACCUM = {"plain": 0, "kahan": 1}
-MAX_BATCH = 32
+MAX_BATCH = 64
 
 # every symbol include/lolaCuda.h declares: (name, restype, argtypes)
 _P = C.c_void_p

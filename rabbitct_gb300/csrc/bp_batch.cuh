@@ -82,7 +82,7 @@ __global__ void __launch_bounds__(32 * LOLA_BATCH_ROWS, LOLA_BATCH_MIN_BLOCKS(S)
 {
   constexpr int VPT = LOLA_BATCH_VPT, ROWS = LOLA_BATCH_ROWS;
   constexpr int TX = LOLA_WARP_X, TY = 32 * ROWS / TX;
-  __shared__ TileProj sp[LOLA_MAX_BATCH];
+  __shared__ TileProj sp[LOLA_BATCH_MAX_WAVE];
   /* the current work item: its job's descriptor and tile, shared by the
      block so the per-voxel loop keeps only what passKernel keeps */
   __shared__ LolaBatchJob J;

@@ -900,7 +900,10 @@ template <int S, int VPT, int ROWS, bool KAHAN, unsigned TEXMASK = PassTexMask<S
 __global__ void __launch_bounds__(32 * ROWS, LOLA_PASS_MIN_BLOCKS(S, VPT, ROWS))
     passKernel(const PassArgs a, const LolaPassParams P)
 {
-  __shared__ TileProj sp[LOLA_MAX_BATCH];
+  /* the per-projection setup of the tile: P.count entries (dynamic shared
+     memory, so that a short pass reserves only what it uses) */
+  extern __shared__ __align__(16) unsigned char passShared[];
+  TileProj *sp = reinterpret_cast<TileProj *>(passShared);
   const int N = P.N;
   /* a warp covers TX x (32 / TX) voxels of the xy plane */
   constexpr int TX = LOLA_WARP_X, TY = 32 * ROWS / TX;
@@ -1013,8 +1016,9 @@ int launchPassShape(const PassArgs &a, const LolaPassParams *P, cudaStream_t str
   const int nz = P->zEnd - P->zBegin;
   constexpr int TX = LOLA_WARP_X, TY = 32 * ROWS / TX;
   const dim3 grid((N + TX - 1) / TX, (N + TY - 1) / TY, (nz + VPT - 1) / VPT);
+  const size_t smem = (size_t)P->count * sizeof(TileProj);
   (void)cudaGetLastError();
-  passKernel<S, VPT, ROWS, KAHAN><<<grid, block, 0, stream>>>(a, *P);
+  passKernel<S, VPT, ROWS, KAHAN><<<grid, block, smem, stream>>>(a, *P);
   return (int)cudaGetLastError();
 }
 

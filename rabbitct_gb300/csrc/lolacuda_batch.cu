@@ -476,7 +476,7 @@ extern "C" int lolaCudaBatchCreate(const LolaCudaJob *jobs, int njobs,
   bt->device = bt->cfg.device;
   bt->njobs = njobs;
   bt->b = bt->cfg.batch;
-  if (bt->b < 1 || bt->b > LOLA_MAX_BATCH || pixelBytes(bt->cfg.storage) == 0 ||
+  if (bt->b < 1 || bt->b > LOLA_BATCH_MAX_WAVE || pixelBytes(bt->cfg.storage) == 0 ||
       (bt->cfg.accumulation != LOLA_ACCUM_PLAIN && bt->cfg.accumulation != LOLA_ACCUM_KAHAN)) {
     delete bt;
     return lolaSetError("batch: invalid configuration");

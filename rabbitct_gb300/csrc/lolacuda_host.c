@@ -1141,7 +1141,7 @@ int lolaCudaAutotune(const LolaCudaGeometry *g, const float *d_images, size_t im
   if (g == NULL || d_images == NULL || h_mats == NULL || cfg == NULL || count <= 0)
     return setError("autotune: invalid arguments");
   static const int shapes[][2] = { { 8, 8 }, { 8, 4 }, { 16, 4 }, { 16, 8 }, { 4, 8 } };
-  static const int batches[] = { 8, 16, 32 };
+  static const int batches[] = { 8, 16, 32, 64 };
   LolaCudaTuneReport local;
   LolaCudaTuneReport *r = report ? report : &local;
   memset(r, 0, sizeof(*r));

@@ -163,6 +163,10 @@ typedef struct {
   int *d_error;           /* device flag set on a wait timeout */
 } LolaStageDesc;
 
+/* Projections per wave of a batched reconstruction (its kernels keep the
+ * wave's per-projection setup in a static shared array of this size). */
+#define LOLA_BATCH_MAX_WAVE 32
+
 /* Work item of the persistent batched pass (bp_batch.cuh): a passKernel tile
  * of LOLA_BATCH_ROWS warps, LOLA_WARP_X x (32 LOLA_BATCH_ROWS / LOLA_WARP_X) x
  * LOLA_BATCH_VPT voxels (the default pass tile, 8 x 16 x 16). */

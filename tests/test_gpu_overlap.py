@@ -147,7 +147,7 @@ def test_edge_batch_is_validated(lib):
     from rabbitct_gb300._native import LolaCudaError
     from rabbitct_gb300.lolacuda import Plan
     vs, o = _geom(16)
-    for edge in (3, 33):
+    for edge in (3, 65):
         with pytest.raises(LolaCudaError, match="edge batch"):
             Plan(16, vs, o, 64, 48, batch=4, edge_batch=edge)
 

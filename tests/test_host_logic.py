@@ -25,7 +25,7 @@ def test_config_validation(lib):
     got = LolaCudaConfig()
     lib.lolaCudaGetConfig(C.byref(got))
     assert (got.storage, got.batch) == (4, 8)
-    for field, value in (("storage", 99), ("batch", 0), ("batch", 33), ("accumulation", 7),
+    for field, value in (("storage", 99), ("batch", 0), ("batch", 65), ("accumulation", 7),
                          ("voxelsPerThread", 3)):
         bad = config(exit_on_error=0)
         setattr(bad, field, value)
@@ -34,10 +34,10 @@ def test_config_validation(lib):
 
 
 def test_edge_batch_validation(lib):
-    """The edge batch is 0 (twice the batch) or batch..32."""
+    """The edge batch is 0 (twice the batch) or batch..64."""
     from rabbitct_gb300._native import config
     for batch, edge, ok in ((16, 0, True), (16, 16, True), (16, 32, True), (16, 15, False),
-                            (16, 33, False), (32, 0, True), (1, 1, True)):
+                            (16, 64, True), (16, 65, False), (32, 0, True), (1, 1, True)):
         c = config(batch=batch, edge_batch=edge, exit_on_error=0)
         assert lib.lolaCudaSetConfig(C.byref(c)) == int(ok), (batch, edge)
         if not ok:
