@@ -256,8 +256,8 @@ int lolaCudaPlanResetStats(LolaCudaPlan *plan);
  * (N, detector) class when batchTune is set; LOLA_BATCH_PERSISTENT runs, per
  * wave of `batch` projections of every job, one pack launch and one
  * persistent pass launch whose blocks pull (job, tile) work items from a
- * counter.  All jobs share the config's storage, accumulation and batch; FP32
- * arithmetic throughout. */
+ * counter.  All jobs share the config's storage, accumulation and batch (at
+ * most 32 projections per wave here); FP32 arithmetic throughout. */
 typedef struct {
   LolaCudaGeometry geometry;   /* whole volume: slice fields must be 0 */
   int32_t projections;
