@@ -453,7 +453,7 @@ struct PassArgs {
   const void *ring;
   size_t slotBytes;
   float *volume;
-  unsigned long long *tileCounters;  /* LOLA_TILE_COUNTERS entries or null */
+  unsigned long long *tileCounters;  /* LOLA_COUNTER_SPREAD x LOLA_TILE_COUNTERS, or null */
   int width, height, margin, pitch, rows;
   unsigned long long tex[LOLA_MAX_BATCH];  /* texture layouts: object per ring slot */
 };
@@ -943,6 +943,9 @@ __global__ void __launch_bounds__(32 * ROWS, LOLA_PASS_MIN_BLOCKS(S, VPT, ROWS))
     loadColumn();
 
   if (a.tileCounters != nullptr && tid == 0) {
+    const unsigned copy =
+        (blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z)) % LOLA_COUNTER_SPREAD;
+    unsigned long long *counters = a.tileCounters + copy * LOLA_TILE_COUNTERS;
     unsigned long long nSkip = 0, nFast = 0, nSlow = 0, nPaired = 0;
     for (int p = 0; p < count; ++p) {
       const int m = sp[p].mode;
@@ -951,10 +954,10 @@ __global__ void __launch_bounds__(32 * ROWS, LOLA_PASS_MIN_BLOCKS(S, VPT, ROWS))
       nSlow += (m == MODE_SLOW);
       nPaired += (m == MODE_FAST && sp[p].pos && LOLA_PAIRED);
     }
-    atomicAdd(a.tileCounters + 0, nSkip);
-    atomicAdd(a.tileCounters + 1, nFast);
-    atomicAdd(a.tileCounters + 2, nSlow);
-    atomicAdd(a.tileCounters + 4, nPaired);
+    atomicAdd(counters + 0, nSkip);
+    atomicAdd(counters + 1, nFast);
+    atomicAdd(counters + 2, nSlow);
+    atomicAdd(counters + 4, nPaired);
   }
 
   const float fi = (float)tx, fj = (float)ty;

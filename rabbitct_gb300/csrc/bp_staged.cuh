@@ -348,11 +348,14 @@ __global__ void __launch_bounds__(32 * (ROWS + 1), LOLA_STAGED_MIN_BLOCKS)
       n[3] += (m == MODE_STAGED);
       n[4] += ((m == MODE_FAST || m == MODE_STAGED) && sp[p].pos && LOLA_PAIRED);
     }
-    atomicAdd(a.tileCounters + 0, n[0]);
-    atomicAdd(a.tileCounters + 1, n[1] + n[3]);
-    atomicAdd(a.tileCounters + 2, n[2]);
-    atomicAdd(a.tileCounters + 3, n[3]);
-    atomicAdd(a.tileCounters + 4, n[4]);
+    const unsigned copy =
+        (blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z)) % LOLA_COUNTER_SPREAD;
+    unsigned long long *counters = a.tileCounters + copy * LOLA_TILE_COUNTERS;
+    atomicAdd(counters + 0, n[0]);
+    atomicAdd(counters + 1, n[1] + n[3]);
+    atomicAdd(counters + 2, n[2]);
+    atomicAdd(counters + 3, n[3]);
+    atomicAdd(counters + 4, n[4]);
   }
 
   if (threadIdx.y == ROWS) {

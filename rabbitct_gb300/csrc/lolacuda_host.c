@@ -418,9 +418,11 @@ static int planInit(LolaCudaPlan *p)
   }
   CUDA_TRY(cudaMalloc((void **)&p->d_stage,
       (size_t)p->ringSlots * p->imageElems * sizeof(float)));
-  CUDA_TRY(cudaMalloc((void **)&p->d_counters, LOLA_TILE_COUNTERS * sizeof(unsigned long long)));
+  CUDA_TRY(cudaMalloc((void **)&p->d_counters,
+      LOLA_COUNTER_SPREAD * LOLA_TILE_COUNTERS * sizeof(unsigned long long)));
   CUDA_TRY(cudaMalloc((void **)&p->d_proj, LOLA_MAX_BATCH * sizeof(LolaPassProj)));
-  CUDA_TRY(cudaMemsetAsync(p->d_counters, 0, LOLA_TILE_COUNTERS * sizeof(unsigned long long),
+  CUDA_TRY(cudaMemsetAsync(p->d_counters, 0,
+      LOLA_COUNTER_SPREAD * LOLA_TILE_COUNTERS * sizeof(unsigned long long),
       p->stream));
   CUDA_TRY(cudaMalloc((void **)&p->d_error, sizeof(int)));
   CUDA_TRY(cudaMemsetAsync(p->d_error, 0, sizeof(int), p->stream));
@@ -1111,8 +1113,11 @@ int lolaCudaPlanGetStats(LolaCudaPlan *p, LolaCudaStats *out)
     return 0;
   if (!collectEvents(p))
     return 0;
+  unsigned long long all[LOLA_COUNTER_SPREAD * LOLA_TILE_COUNTERS];
+  CUDA_TRY(cudaMemcpy(all, p->d_counters, sizeof(all), cudaMemcpyDeviceToHost));
   unsigned long long c[LOLA_TILE_COUNTERS] = { 0, 0, 0, 0, 0 };
-  CUDA_TRY(cudaMemcpy(c, p->d_counters, sizeof(c), cudaMemcpyDeviceToHost));
+  for (int i = 0; i < LOLA_COUNTER_SPREAD * LOLA_TILE_COUNTERS; i++)
+    c[i % LOLA_TILE_COUNTERS] += all[i];
   p->stats.tilePassesSkipped = (int64_t)c[0];
   p->stats.tilePassesFast = (int64_t)c[1];
   p->stats.tilePassesSlow = (int64_t)c[2];
@@ -1129,7 +1134,8 @@ int lolaCudaPlanResetStats(LolaCudaPlan *p)
   if (!lolaCudaPlanSynchronize(p) || !collectEvents(p))
     return 0;
   memset(&p->stats, 0, sizeof(p->stats));
-  CUDA_TRY(cudaMemset(p->d_counters, 0, LOLA_TILE_COUNTERS * sizeof(unsigned long long)));
+  CUDA_TRY(cudaMemset(p->d_counters, 0,
+      LOLA_COUNTER_SPREAD * LOLA_TILE_COUNTERS * sizeof(unsigned long long)));
   return 1;
 }
 

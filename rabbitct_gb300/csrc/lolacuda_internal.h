@@ -91,6 +91,10 @@ typedef struct {
 /* Per-plan tile counters of the pass kernels: (tile, projection) pairs
  * skipped, fast (staged included), slow, staged, and fast on the paired path. */
 #define LOLA_TILE_COUNTERS 5
+/* Copies of the counters the pass kernels spread their atomic adds over
+ * (block index modulo this): one set per plan would have every block's adds
+ * meet at four addresses.  The host sums the copies. */
+#define LOLA_COUNTER_SPREAD 64
 
 /* Mixed layouts: voxels (bit k of a thread's column) that fetch through the
  * texture unit.  Row-ordered quads (f32qx, and f16qx with LOLA_F16QX_COLS 0):
