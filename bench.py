@@ -19,7 +19,9 @@ Lines printed (rank 0, one JSON object):
           finish with the volume copied back), wall clock around the calls,
           median of --e2e-steps
   roofline  the pass kernel against the measured HBM copy bandwidth
-          (MEASURED_PEAKS.json): algorithmic bytes per launch / launch time,
+          (MEASURED_PEAKS.json), from one instrumented reconstruction after
+          the (uninstrumented) timed steps: algorithmic bytes per launch /
+          launch time (CUDA events around every pass),
           and the DRAM bytes of one launch from the committed ncu capture of
           the same configuration; `ceiling` holds the bound the kernel meets,
           the gather and FP32-issue rates measured by probe kernels on the
@@ -400,7 +402,10 @@ def time_device(args, dist, lib_mod, scan, vs, o, d_images, storage, clocks=None
     from rabbitct_gb300.lolacuda import Plan
     W, H = scan.width, scan.height
     cfg, tried = tuned_config(args, dist, scan, vs, o, d_images, storage)
-    cfg.collectStats = 1
+    # the timed steps run uninstrumented; the per-launch times and the tile
+    # counters of the roofline come from one more reconstruction afterwards
+    # with statistics on (events around every pass, counters in the kernel)
+    cfg.collectStats = 0
     with Plan(args.n, vs, o, W, H, cfg=cfg, slab=my_slab(args, dist)) as p:
         for _ in range(args.warmup):
             p.zero()
@@ -419,6 +424,15 @@ def time_device(args, dist, lib_mod, scan, vs, o, d_images, storage, clocks=None
         clk = clocks.stop() if clocks is not None else None
         p.synchronize()
         dist.barrier()
+        launches = p.stats()
+    cfg.collectStats = 1
+    with Plan(args.n, vs, o, W, H, cfg=cfg, slab=my_slab(args, dist)) as p:
+        p.backproject_device(d_images.ptr, W * H, scan.matrices)
+        p.synchronize()
+        p.reset_stats()
+        p.zero()
+        p.backproject_device(d_images.ptr, W * H, scan.matrices)
+        p.synchronize()
         st = p.stats()
     ms_max = dist.max(ms)
     updates = total_updates(args, scan, dist) * args.steps
@@ -427,7 +441,7 @@ def time_device(args, dist, lib_mod, scan, vs, o, d_images, storage, clocks=None
               "autotuned": bool(args.autotune),
               "candidates_timed": 0 if tried is None else sum(1 for t in tried if t[3] > 0)}
     return {"ms": ms_max, "gups": updates / (ms_max * 1e-3) / 1e9, "stats": st, "clocks": clk,
-            "cfg": cfg, "chosen": chosen}
+            "cfg": cfg, "chosen": chosen, "launches": launches.passes + launches.packs}
 
 
 def roofline(args, lib, storage, st, probes, cfg=None) -> dict:
@@ -706,7 +720,7 @@ def run_gpu(args, rank, world, local):
         "dtype": "f32",
         "data": "synthetic (seeded ellipsoid phantom, RabbitCT shapes)",
         "config": workload_config(args, args.storage),
-        "gpu_launches": int(st.passes + st.packs),
+        "gpu_launches": int(head["launches"]),
         "clocks": head["clocks"],
         "roofline": roofline(args, lib, args.storage, st, probes, head["cfg"]),
         "tuned": head["chosen"],
