@@ -23,31 +23,49 @@ struct ImageGeom {
   int width, height, margin, pitch, rows;
 };
 
-template <int S>
-__global__ void __launch_bounds__(256) batchPackKernel(const LolaBatchWave w)
+/* The image geometry of batchParamPassKernel: ImageGeom plus the texel index
+   of the projection's slot within its job's one texture. */
+struct SlotGeom {
+  int width, height, margin, pitch, rows;
+  uint32_t texBase;
+};
+
+template <> __device__ __forceinline__ uint32_t texIndexBase<SlotGeom>(const SlotGeom &a)
 {
-  const int pair = blockIdx.z;
+  return a.texBase;
+}
+
+/* Stores one wave: block (pair, r) packs rows r, r + LOLA_BATCH_PACK_ROWS, ...
+   of the stored image of pair = (job, slot), 256 columns at a time, so that
+   the grid covers each job's own image and no more (a grid over the largest
+   image for every pair left most blocks of the small detectors idle). */
+#define LOLA_BATCH_PACK_ROWS 64
+template <int S>
+__global__ void __launch_bounds__(256) batchPackKernel(const __grid_constant__ LolaBatchWave w)
+{
+  const int pair = blockIdx.x;
   const int j = pair / w.b, slot = pair - j * w.b;
   const LolaBatchJob &J = w.jobs[j];
   const int view = w.wave * w.b + slot;
   if (view >= J.nproj)
     return;
-  const int pu = blockIdx.x * 32 + threadIdx.x;
-  const int pv = blockIdx.y * 8 + threadIdx.y;
-  if (pu >= J.pitch || pv >= J.rows)
-    return;
   const float *img = J.images + (size_t)view * J.width * J.height;
-  const int u = pu - J.margin, v = pv - J.margin;
   auto px = [&](int uu, int vv) -> float {
     return (uu >= 0 && uu < J.width && vv >= 0 && vv < J.height)
                ? __ldg(img + (size_t)vv * J.width + uu)
                : 0.0f;
   };
-  const size_t o = (size_t)slot * J.slotElems + (size_t)pv * J.pitch + pu;
-  if constexpr (Layout<S>::kQuad)
-    Layout<S>::store(J.ring, o, px(u, v), px(u + 1, v), px(u, v + 1), px(u + 1, v + 1));
-  else
-    Layout<S>::store(J.ring, o, px(u, v), 0.f, 0.f, 0.f);
+  for (int pv = blockIdx.y; pv < J.rows; pv += LOLA_BATCH_PACK_ROWS) {
+    const int v = pv - J.margin;
+    for (int pu = threadIdx.x; pu < J.pitch; pu += 256) {
+      const int u = pu - J.margin;
+      const size_t o = (size_t)slot * J.slotElems + (size_t)pv * J.pitch + pu;
+      if constexpr (Layout<S>::kQuad)
+        Layout<S>::store(J.ring, o, px(u, v), px(u + 1, v), px(u, v + 1), px(u + 1, v + 1));
+      else
+        Layout<S>::store(J.ring, o, px(u, v), 0.f, 0.f, 0.f);
+    }
+  }
 }
 
 /* Resident blocks per SM for the batched pass; its per-job geometry lives in
@@ -182,11 +200,116 @@ __global__ void __launch_bounds__(32 * LOLA_BATCH_ROWS, LOLA_BATCH_MIN_BLOCKS(S)
   }
 }
 
+/* The persistent pass from the wave's kernel parameters (LolaBatchWave.pj,
+   up to LOLA_BATCH_PARAM_JOBS jobs): the work item's job, tile and
+   geometry are uniform values of the parameter space, as in passKernel, so
+   f16qx fetches every quad through its job's one linear texture (at the
+   slot's texel offset) like passKernel does; no job descriptor is copied to
+   shared memory. */
+template <int S> struct ParamTexMask {
+  static constexpr unsigned kValue = S == LOLA_STORE_F16QX ? LOLA_F16QX_TEX_MASK : 0u;
+};
+
+template <int S, bool KAHAN>
+__global__ void __launch_bounds__(32 * LOLA_BATCH_ROWS,
+    (MinBlocks<S, LOLA_BATCH_VPT, LOLA_BATCH_ROWS>::kValue))
+    batchParamPassKernel(const __grid_constant__ LolaBatchWave w)
+{
+  constexpr int VPT = LOLA_BATCH_VPT, ROWS = LOLA_BATCH_ROWS;
+  constexpr int TX = LOLA_WARP_X, TY = 32 * ROWS / TX;
+  constexpr unsigned TEXMASK = ParamTexMask<S>::kValue;
+  __shared__ TileProj sp[LOLA_BATCH_MAX_WAVE];
+  __shared__ long long sItem;
+  const int tid = threadIdx.y * 32 + threadIdx.x;
+  const int tx = threadIdx.x % TX, ty = threadIdx.y * (32 / TX) + threadIdx.x / TX;
+  const float fi = (float)tx, fj = (float)ty;
+  for (;;) {
+    if (tid == 0)
+      sItem = atomicAdd(w.counter, 1);
+    __syncthreads();
+    const long long item = sItem;
+    if (item >= w.totalItems)
+      break;
+    /* job of the item: the last j with pj[j].firstItem <= item */
+    int lo = 0, hi = w.njobs - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (w.pj[mid].firstItem <= item)
+        lo = mid;
+      else
+        hi = mid - 1;
+    }
+    const LolaBatchParamJob &J = w.pj[lo];
+    const int count = min(w.b, J.count);
+    if (count > 0) {
+      long long t = item - J.firstItem;
+      const int x0 = (int)(t % J.tilesX) * TX;
+      t /= J.tilesX;
+      const int y0 = (int)(t % J.tilesY) * TY;
+      const int z0 = (int)(t / J.tilesY) * VPT;
+      TileGeom g;
+      g.N = J.N;
+      g.zEnd = J.N;
+      g.voxelSize = J.voxelSize;
+      g.originIndex = J.originIndex;
+      g.width = J.width;
+      g.height = J.height;
+      g.margin = LOLA_MARGIN;
+      setupTileGeom<ROWS, VPT, TX>(w.proj + (size_t)lo * w.b, count, g, sp, tid, 32 * ROWS, x0,
+          y0, z0);
+      const int N = J.N;
+      const int x = x0 + tx, y = y0 + ty;
+      const bool inXY = (x < N) && (y < N);
+      const size_t slice = (size_t)N * (size_t)N;
+      float2 acc[VPT / 2], comp[VPT / 2];
+      {
+        const float *vcol = J.volume + ((size_t)z0 * N + (size_t)(inXY ? y : 0)) * (size_t)N +
+                            (inXY ? x : 0);
+#pragma unroll
+        for (int k = 0; k < VPT; ++k) {
+          voxel(acc, k) = (inXY && z0 + k < N) ? vcol[k * slice] : 0.0f;
+          voxel(comp, k) = 0.0f;
+        }
+      }
+      for (int p = 0; p < count; ++p) {
+        const int mode = sp[p].mode;
+        if (mode == MODE_SKIP)
+          continue;
+        const TileProj tp = sp[p];
+        SlotGeom a;
+        a.width = J.width;
+        a.height = J.height;
+        a.margin = LOLA_MARGIN;
+        a.pitch = J.pitch;
+        a.rows = J.rows;
+        a.texBase = (uint32_t)tp.slot * J.slotElems;
+        const void *img = J.ring + (size_t)tp.slot * J.slotBytes;
+        const unsigned long long tex = J.tex;
+        if (mode == MODE_FAST && tp.pos && LOLA_PAIRED && LOLA_BATCH_PAIRED)
+          applyPairs<S, VPT, KAHAN, SlotGeom, TEXMASK>(tp, img, tex, a, fi, fj, acc, comp);
+        else if (mode == MODE_FAST)
+          applyProjection<S, VPT, KAHAN, false, SlotGeom, TEXMASK>(tp, img, tex, a, fi, fj,
+              acc, comp);
+        else
+          applyProjection<S, VPT, KAHAN, true, SlotGeom, TEXMASK>(tp, img, tex, a, fi, fj,
+              acc, comp);
+      }
+      float *vcol = J.volume + ((size_t)z0 * N + (size_t)(inXY ? y : 0)) * (size_t)N +
+                    (inXY ? x : 0);
+#pragma unroll
+      for (int k = 0; k < VPT; ++k)
+        if (inXY && z0 + k < N)
+          vcol[k * slice] = KAHAN ? (voxel(acc, k) - voxel(comp, k)) : voxel(acc, k);
+    }
+    __syncthreads(); /* sp[] and sItem are rewritten next */
+  }
+}
+
 template <int S>
 int launchBatchPack(const LolaBatchWave *w, cudaStream_t stream)
 {
-  const dim3 block(32, 8);
-  const dim3 grid((w->maxPitch + 31) / 32, (w->maxRows + 7) / 8, w->njobs * w->b);
+  const dim3 block(256);
+  const dim3 grid(w->njobs * w->b, LOLA_BATCH_PACK_ROWS);
   (void)cudaGetLastError();  /* report this launch's error, not an earlier one */
   batchPackKernel<S><<<grid, block, 0, stream>>>(*w);
   return (int)cudaGetLastError();
@@ -197,16 +320,31 @@ int launchBatchPass(const LolaBatchWave *w, int blocks, cudaStream_t stream)
 {
   const dim3 block(32, LOLA_BATCH_ROWS);
   (void)cudaGetLastError();  /* report this launch's error, not an earlier one */
-  if (w->accumulation == LOLA_ACCUM_KAHAN)
-    batchPassKernel<S, true><<<blocks, block, 0, stream>>>(*w);
-  else
-    batchPassKernel<S, false><<<blocks, block, 0, stream>>>(*w);
+  const bool kahan = w->accumulation == LOLA_ACCUM_KAHAN;
+  if (w->paramJobs) {
+    if (kahan)
+      batchParamPassKernel<S, true><<<blocks, block, 0, stream>>>(*w);
+    else
+      batchParamPassKernel<S, false><<<blocks, block, 0, stream>>>(*w);
+  } else {
+    if (kahan)
+      batchPassKernel<S, true><<<blocks, block, 0, stream>>>(*w);
+    else
+      batchPassKernel<S, false><<<blocks, block, 0, stream>>>(*w);
+  }
   return (int)cudaGetLastError();
 }
 
 template <int S>
-int batchOccupancy(int accumulation, int *blocks)
+int batchOccupancy(int accumulation, int paramJobs, int *blocks)
 {
+  const int threads = 32 * LOLA_BATCH_ROWS;
+  if (paramJobs)
+    return (int)(accumulation == LOLA_ACCUM_KAHAN
+                     ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks,
+                           batchParamPassKernel<S, true>, threads, 0)
+                     : cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks,
+                           batchParamPassKernel<S, false>, threads, 0));
   cudaError_t e = accumulation == LOLA_ACCUM_KAHAN
                       ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(
                             blocks, batchPassKernel<S, true>, 32 * LOLA_BATCH_ROWS, 0)

@@ -397,6 +397,12 @@ __device__ __forceinline__ void texQuadLinear(unsigned long long tex, uint32_t i
   p11 = q.w;
 }
 
+/* Texel index of a projection's first stored pixel within its linear
+   texture: 0 where each ring slot has a texture of its own (the pass kernel's
+   geometry), the slot's offset where one texture spans a job's slots (the
+   batched pass's SlotGeom, bp_batch.cuh). */
+template <class A> __device__ __forceinline__ uint32_t texIndexBase(const A &) { return 0u; }
+
 /* ---- packing: FP32 detector image -> zero-padded stored layout ------------- */
 
 struct PackArgs {
@@ -515,7 +521,7 @@ __device__ __forceinline__ void applyProjection(const TileProj &tp, const void *
       if (LOLA_MIXED_TEX_LINEAR) {
         /* the texel at the load path's index; any index past the slot reads 0 */
         const uint32_t idx = __float_as_uint(fmaf(ty, pitchF, tx + biasF)) - 0x4B000000u;
-        texQuadLinear<Layout<S>::kCols>(tex, idx, p00, p10, p01, p11);
+        texQuadLinear<Layout<S>::kCols>(tex, idx + texIndexBase(a), p00, p10, p01, p11);
       } else {
         /* point fetch of texel (tx + M, ty + M): any coordinate inside it works */
         const float off = (float)a.margin + 0.5f;
@@ -703,7 +709,7 @@ __device__ __forceinline__ void applyPairs(const TileProj &tp, const void *img,
       if (Layout<S>::kMixed && ((TEXMASK >> k) & 1u)) {
         if (LOLA_MIXED_TEX_LINEAR) {
           /* an index past the slot reads 0: no clamp needed for memory safety */
-          const uint32_t idx = __float_as_uint(idxf) - 0x4B000000u;
+          const uint32_t idx = __float_as_uint(idxf) - 0x4B000000u + texIndexBase(a);
           if ((COLSMASK >> k) & 1u)
             texQuadLinear<Layout<S>::kCols, true>(tex, idx, p00, p10, p01, p11);
           else
@@ -1092,7 +1098,7 @@ int launchPass(const LolaStoreDesc *st, const LolaPassParams *P, const void *rin
   {                                                                                        \
     return lola::launchBatchPass<S>(w, blocks, static_cast<cudaStream_t>(stream));         \
   }                                                                                        \
-  extern "C" int lolaBatchOccupancy_##NAME(int accumulation, int *blocks)                  \
+  extern "C" int lolaBatchOccupancy_##NAME(int accumulation, int paramJobs, int *blocks)   \
   {                                                                                        \
-    return lola::batchOccupancy<S>(accumulation, blocks);                                  \
+    return lola::batchOccupancy<S>(accumulation, paramJobs, blocks);                       \
   }

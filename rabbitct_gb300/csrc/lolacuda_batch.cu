@@ -424,7 +424,37 @@ int build(LolaCudaBatch *bt, const LolaCudaJob *jobs)
   /* persistent grid: every resident slot of the GPU */
   int sms = 0, perSM = 0;
   BT_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, bt->device));
-  int rc = lolaBatchPassOccupancy(storage, bt->cfg.accumulation, &perSM);
+  /* the jobs in each wave's kernel parameters (batchParamPassKernel) when they
+     fit there, for the layouts read by loads or, f16qx, through one linear
+     texture over each job's slots */
+  int paramJobs = nj <= LOLA_BATCH_PARAM_JOBS && ch != 1;
+  std::vector<unsigned long long> jobTex(nj, 0ull);
+  if (paramJobs && storage == LOLA_STORE_F16QX) {
+    int maxLinear = 0;
+    BT_TRY(cudaDeviceGetAttribute(&maxLinear, cudaDevAttrMaxTexture1DLinearWidth, bt->device));
+    for (int j = 0; j < nj; ++j)
+      if ((double)b * (double)hj[j].slotElems > (double)maxLinear ||
+          (double)b * (double)hj[j].slotElems >= 4294967296.0)
+        paramJobs = 0;
+    for (int j = 0; paramJobs && j < nj; ++j) {
+      cudaResourceDesc rd;
+      memset(&rd, 0, sizeof(rd));
+      rd.resType = cudaResourceTypeLinear;
+      rd.res.linear.devPtr = bt->d_ring + ringOffset[j];
+      rd.res.linear.desc = cudaCreateChannelDesc(16, 16, 16, 16, cudaChannelFormatKindFloat);
+      rd.res.linear.sizeInBytes = (size_t)b * hj[j].slotBytes;
+      cudaTextureDesc td;
+      memset(&td, 0, sizeof(td));
+      td.addressMode[0] = cudaAddressModeBorder;
+      td.filterMode = cudaFilterModePoint;
+      td.readMode = cudaReadModeElementType;
+      cudaTextureObject_t t = 0;
+      BT_TRY(cudaCreateTextureObject(&t, &rd, &td, nullptr));
+      bt->textures.push_back(t);
+      jobTex[j] = (unsigned long long)t;
+    }
+  }
+  int rc = lolaBatchPassOccupancy(storage, bt->cfg.accumulation, paramJobs, &perSM);
   if (rc != 0 || perSM <= 0)
     return lolaSetError("batch: occupancy query failed (%d)", rc);
   bt->blocks = sms * perSM;
@@ -435,6 +465,28 @@ int build(LolaCudaBatch *bt, const LolaCudaJob *jobs)
   cudaError_t me = cudaMemsetAsync(bt->d_counters, 0, (size_t)W * sizeof(int), bt->stream);
   for (int w = 0; w < W && me == cudaSuccess && launchRc == 0; ++w) {
     LolaBatchWave wa;
+    memset(&wa, 0, sizeof(wa));
+    wa.paramJobs = paramJobs;
+    for (int j = 0; paramJobs && j < nj; ++j) {
+      const LolaBatchJob &J = hj[j];
+      LolaBatchParamJob &q = wa.pj[j];
+      q.volume = J.volume;
+      q.ring = J.ring;
+      q.tex = jobTex[j];
+      q.firstItem = prefix[(size_t)w * (nj + 1) + j];
+      q.slotBytes = J.slotBytes;
+      q.slotElems = (uint32_t)J.slotElems;
+      q.count = J.nproj - w * b;
+      q.N = J.N;
+      q.width = J.width;
+      q.height = J.height;
+      q.pitch = J.pitch;
+      q.rows = J.rows;
+      q.tilesX = J.tilesX;
+      q.tilesY = J.tilesY;
+      q.voxelSize = J.voxelSize;
+      q.originIndex = J.originIndex;
+    }
     wa.jobs = bt->d_jobs;
     wa.tilePrefix = bt->d_prefix + (size_t)w * (nj + 1);
     wa.proj = bt->d_proj + (size_t)w * nj * b;

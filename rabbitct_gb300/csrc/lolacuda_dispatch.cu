@@ -10,7 +10,7 @@
       const LolaStageDesc *, const void *, float *, unsigned long long *, void *);         \
   extern "C" int lolaLaunchBatchPack_##NAME(const LolaBatchWave *, void *);                \
   extern "C" int lolaLaunchBatchPass_##NAME(const LolaBatchWave *, int, void *);           \
-  extern "C" int lolaBatchOccupancy_##NAME(int, int *);
+  extern "C" int lolaBatchOccupancy_##NAME(int, int, int *);
 
 LOLA_DECLARE(F32)
 LOLA_DECLARE(F16)
@@ -106,9 +106,9 @@ extern "C" int lolaLaunchBatchPass(const LolaBatchWave *w, int blocks, void *str
 #undef PASS_CALL
 }
 
-extern "C" int lolaBatchPassOccupancy(int storage, int accumulation, int *blocks)
+extern "C" int lolaBatchPassOccupancy(int storage, int accumulation, int paramJobs, int *blocks)
 {
-#define OCC_CALL(NAME) lolaBatchOccupancy_##NAME(accumulation, blocks)
+#define OCC_CALL(NAME) lolaBatchOccupancy_##NAME(accumulation, paramJobs, blocks)
   LOLA_BATCH_CASES(OCC_CALL)
 #undef OCC_CALL
 }

@@ -190,6 +190,24 @@ typedef struct {
   int32_t tilesX, tilesY, tilesZ, nproj;
 } LolaBatchJob;
 
+/* A job as the persistent pass reads it from its wave's kernel parameters
+ * (LolaBatchWave.pj): every per-item value uniform, as passKernel's are. */
+typedef struct {
+  float *volume;                    /* N^3 FP32 */
+  const unsigned char *ring;        /* this job's `b` stored slots */
+  unsigned long long tex;           /* f16qx: one linear texture over the slots, else 0 */
+  long long firstItem;              /* the job's first work item in this wave */
+  size_t slotBytes;
+  uint32_t slotElems;
+  int32_t count;                    /* projections of this wave (<= 0: none) */
+  int32_t N, width, height, pitch, rows, tilesX, tilesY;
+  float voxelSize, originIndex;
+} LolaBatchParamJob;
+
+/* Jobs a wave carries in its kernel parameters; batches of more jobs run the
+ * persistent pass from the device job table instead. */
+#define LOLA_BATCH_PARAM_JOBS 128
+
 /* One wave of a batch: projections [wave*b, wave*b + b) of every job. */
 typedef struct {
   const LolaBatchJob *jobs;         /* device, njobs */
@@ -198,6 +216,8 @@ typedef struct {
   int *counter;                     /* device: this wave's work-item counter */
   long long totalItems;
   int32_t njobs, b, wave, maxPitch, maxRows, accumulation, storage;
+  int32_t paramJobs;                /* 1: pj[0 .. njobs) holds the jobs */
+  LolaBatchParamJob pj[LOLA_BATCH_PARAM_JOBS];
 } LolaBatchWave;
 
 /* Kernel launchers (lolacuda_dispatch.cu).  Return 0 on success or a
@@ -225,7 +245,7 @@ int lolaSetError(const char *fmt, ...);
 int lolaLaunchBatchPack(const LolaBatchWave *wave, void *stream);
 int lolaLaunchBatchPass(const LolaBatchWave *wave, int blocks, void *stream);
 /* Resident blocks per SM of the batched pass for a storage layout. */
-int lolaBatchPassOccupancy(int storage, int accumulation, int *blocksPerSM);
+int lolaBatchPassOccupancy(int storage, int accumulation, int paramJobs, int *blocksPerSM);
 
 /* 1 if the (voxelsPerThread, rowsPerBlock) pair has a compiled kernel. */
 int lolaKernelShapeSupported(int voxelsPerThread, int rowsPerBlock);

@@ -113,3 +113,38 @@ def test_autotune_picks_a_measured_candidate(scans):
     d_img.free()
     ref = oracle.bunny_f64(n, vs, o, scan.matrices, scan.images)
     assert metrics.errors(vol, ref)["rel_rmse"] <= 1e-3
+
+
+@pytest.mark.parametrize("storage", ["f16qx", "f32"])
+def test_persistent_batch_of_more_jobs_than_the_wave_parameters_hold(storage):
+    """130 small jobs, more than a wave's kernel parameters carry (128): the
+    persistent pass then reads the jobs from the device job table (mixed
+    layouts by loads).  Same volumes as one plan per job."""
+    from rabbitct_gb300 import build as b
+    b.build_lolacuda()
+    from rabbitct_gb300.lolacuda import Batch, DeviceBuffer, Plan
+    cases = []
+    for j in range(130):
+        n = 8 + (j % 3) * 4
+        scan = synth.make_scan(small_spec(nproj=2 + j % 3, width=24, height=20, seed=400 + j))
+        vs = 256.0 / n
+        cases.append((n, vs, synth.origin_index(n, vs), scan))
+    bufs, jobs = [], []
+    for n, vs, o, scan in cases:
+        d_img = DeviceBuffer.from_array(scan.images)
+        d_vol = DeviceBuffer.from_array(np.zeros((n, n, n), np.float32))
+        bufs.append((d_img, d_vol))
+        jobs.append(dict(n=n, voxel_size=vs, origin_index=o, width=scan.width,
+                         height=scan.height, d_images=d_img.ptr, matrices=scan.matrices,
+                         d_volume=d_vol.ptr))
+    with Batch(jobs, storage=storage, batch=4, batch_mode=1) as bt:
+        bt.run()
+        bt.synchronize()
+        got = [v.to_array((n, n, n), np.float32) for (_, v), (n, *_r) in zip(bufs, cases)]
+    for (n, vs, o, scan), g in zip(cases, got):
+        with Plan(n, vs, o, scan.width, scan.height, storage=storage, batch=4) as plan:
+            plan.backproject_host(scan.images, scan.matrices)
+            assert np.array_equal(g, plan.download()), (n, storage)
+    for d_img, d_vol in bufs:
+        d_img.free()
+        d_vol.free()
