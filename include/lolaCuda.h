@@ -452,10 +452,11 @@ int lolaCudaHostFree(void *h_ptr);
 double lolaCudaProbeIssueRate(void);
 /* Voxel updates per second that the pass kernel's 2x2 gather pattern alone
  * sustains for a storage layout over a padded width x height detector, at
- * random positions (L2-resident, no reuse in L1). */
+ * random positions (L2-resident, no reuse in L1): lanes 1.25 px apart, four
+ * independent fetches per thread and step, two rows apart. */
 double lolaCudaProbeGatherRate(int storage, int width, int height);
 /* The same fetches inside an image small enough to stay in every SM's L1:
- * the rate of the gather pipes themselves, an upper bound for any pattern. */
+ * the rate of the gather pipes themselves for this lane spacing. */
 double lolaCudaProbeGatherPeak(int storage);
 /* SM count, SM clock (kHz) and name of the current device. */
 int lolaCudaDeviceInfo(int *smCount, int *clockKHz, char *name, int nameLen);

@@ -106,7 +106,8 @@ __global__ void __launch_bounds__(32 * LOLA_BATCH_ROWS, LOLA_BATCH_MIN_BLOCKS(S)
   __shared__ LolaBatchJob J;
   __shared__ int itemJob, itemCount, itemX0, itemY0, itemZ0, itemDone;
   const int tid = threadIdx.y * 32 + threadIdx.x;
-  const int tx = threadIdx.x % TX, ty = threadIdx.y * (32 / TX) + threadIdx.x / TX;
+  int tx, ty;
+  laneVoxel<TX, LaneGroups<S>::kValue>(threadIdx.x, threadIdx.y, tx, ty);
   const float fi = (float)tx, fj = (float)ty;
   for (;;) {
     if (tid == 0) {
@@ -221,7 +222,8 @@ __global__ void __launch_bounds__(32 * LOLA_BATCH_ROWS,
   __shared__ TileProj sp[LOLA_BATCH_MAX_WAVE];
   __shared__ long long sItem;
   const int tid = threadIdx.y * 32 + threadIdx.x;
-  const int tx = threadIdx.x % TX, ty = threadIdx.y * (32 / TX) + threadIdx.x / TX;
+  int tx, ty;
+  laneVoxel<TX, LaneGroups<S>::kValue>(threadIdx.x, threadIdx.y, tx, ty);
   const float fi = (float)tx, fj = (float)ty;
   for (;;) {
     if (tid == 0)

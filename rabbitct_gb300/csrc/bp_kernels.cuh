@@ -733,6 +733,43 @@ __device__ __forceinline__ void applyPairs(const TileProj &tp, const void *img,
       acc, comp);
 }
 
+/* Lane -> voxel within a warp's TX x (32 / TX) patch of the xy plane.  The
+ * texture unit (and the L1 for quad loads) serves a warp's fetch in 8-lane
+ * quarters, one data-stage wavefront for each detector row (or 128-byte
+ * window) that a quarter's eight texels touch.  The voxels of one quarter
+ * project to the same detector row unless their depths along the ray
+ * differ (the magnification then moves them up to about a pixel per 8
+ * voxels at the detector's top and bottom), so GROUPS gives each quarter a
+ * 4 x 2 patch instead of a row of 8 voxels: its depth spread is
+ * 3|sin a| + |cos a| voxels instead of 7|sin a| over the ray angle a, and
+ * it straddles a row boundary about half as often (f16qx at N=1024: 1.63
+ * wavefronts per quarter with rows of 8; 1775 -> 1868 GUPS with 4 x 2
+ * quarters, bit-identical volumes).  Without GROUPS the warp's lanes run
+ * along x row by row. */
+#ifndef LOLA_LANE_GROUPS
+#define LOLA_LANE_GROUPS -1  /* -1: per storage (LaneGroups); 0: never; 1: always */
+#endif
+template <int S> struct LaneGroups {
+  /* measured at N=1024 on GB300 (the other layouts within +-0.8 % either
+     way, so they keep rows of 8): f16qx +5 %, f32q +2.6 % */
+  static constexpr bool kValue =
+      LOLA_LANE_GROUPS < 0 ? (S == LOLA_STORE_F16QX || S == LOLA_STORE_F32Q)
+                           : LOLA_LANE_GROUPS != 0;
+};
+
+template <int TX, bool GROUPS>
+__device__ __forceinline__ void laneVoxel(int lane, int warp, int &tx, int &ty)
+{
+  if (GROUPS && TX == 8) {
+    const int q = lane >> 3, j = lane & 7;  /* quarter, lane in the quarter */
+    tx = (q & 1) * 4 + (j & 3);
+    ty = warp * 4 + (q >> 1) * 2 + (j >> 2);
+  } else {
+    tx = lane % TX;
+    ty = warp * (32 / TX) + lane / TX;
+  }
+}
+
 /* Per-(tile, projection) setup shared by the pass kernels: the FP64 tile
  * origin (phase A, one thread per projection) and the footprint and mode from
  * the 8 tile corners (phase B, 8 lanes per projection).  Ends with the block
@@ -923,7 +960,8 @@ __global__ void __launch_bounds__(32 * ROWS, LOLA_PASS_MIN_BLOCKS(S, VPT, ROWS))
      are issued before the setup, so that their latency overlaps the setup's
      (f32 +1.3 %, f32q +0.9 % at N=1024 on GB300); for the 16-bit layouts,
      whose registers are fuller, after it (f16qx 1 % faster that way) */
-  const int tx = threadIdx.x % TX, ty = threadIdx.y * (32 / TX) + threadIdx.x / TX;
+  int tx, ty;
+  laneVoxel<TX, LaneGroups<S>::kValue>(threadIdx.x, threadIdx.y, tx, ty);
   const int x = x0 + tx, y = y0 + ty;
   const bool inXY = (x < N) && (y < N);
   const size_t slice = (size_t)N * (size_t)N;

@@ -304,7 +304,7 @@ int build(LolaCudaBatch *bt, const LolaCudaJob *jobs)
     J.width = g.imageWidth;
     J.height = g.imageHeight;
     J.margin = LOLA_MARGIN;
-    J.pitch = (g.imageWidth + 2 * LOLA_MARGIN + 31) & ~31;
+    J.pitch = lolaStorePitch(g.imageWidth, storage, pix);
     J.rows = g.imageHeight + 2 * LOLA_MARGIN;
     if ((long long)J.pitch * J.rows >= (1LL << 23) - 2 * (long long)J.pitch)
       return lolaSetError("batch: job %d detector %dx%d too large", j, g.imageWidth,

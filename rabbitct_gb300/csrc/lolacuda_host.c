@@ -347,9 +347,7 @@ static int planInit(LolaCudaPlan *p)
   s->margin = LOLA_MARGIN;
   s->width = g->imageWidth;
   s->height = g->imageHeight;
-  /* pitch a multiple of 32 pixels: row starts stay 64 B aligned for every
-     element size, which texture fetches from pitched memory require */
-  s->pitch = (g->imageWidth + 2 * LOLA_MARGIN + 31) & ~31;
+  s->pitch = lolaStorePitch(g->imageWidth, s->storage, s->elemBytes);
   s->rows = g->imageHeight + 2 * LOLA_MARGIN;
   /* index arithmetic in the kernel is exact below 2^23 pixels */
   if ((long long)s->pitch * s->rows >= (1LL << 23) - 2 * (long long)s->pitch)

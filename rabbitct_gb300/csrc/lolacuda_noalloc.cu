@@ -216,8 +216,8 @@ extern "C" int lolaCudaBackprojectNoAlloc(const LolaCudaGeometry *g, const LolaC
   st.margin = LOLA_MARGIN;
   st.width = g->imageWidth;
   st.height = g->imageHeight;
-  /* the plan's layout: pitch a multiple of 32 pixels, slots 256 pixels apart */
-  st.pitch = (g->imageWidth + 2 * LOLA_MARGIN + 31) & ~31;
+  /* the plan's layout: its pitch, slots 256 pixels apart */
+  st.pitch = lolaStorePitch(g->imageWidth, st.storage, eb);
   st.rows = g->imageHeight + 2 * LOLA_MARGIN;
   st.reserved = 0;
   if ((long long)st.pitch * st.rows >= (1LL << 23) - 2 * (long long)st.pitch)

@@ -8,11 +8,14 @@
  *          each warp reads, for 32 lanes at detector columns spaced 1.25 px
  *          apart, the 2x2 taps of a stored projection, in the kernel's storage
  *          layouts (4 x 4 B, 4 x 2 B, 1 x 16 B or 1 x 8 B per update, or one
- *          texel fetch).  Returns updates / s the gather path alone sustains:
+ *          texel fetch).  Each thread issues four independent fetches per
+ *          step, two detector rows apart (as a thread's voxels along z
+ *          project), so the rate is that of the pipes and not of one fetch's
+ *          latency.  Returns updates / s the gather path alone sustains:
  *          lolaCudaProbeGatherRate at random positions of a full-size,
  *          L2-resident projection (no reuse in L1), lolaCudaProbeGatherPeak
  *          inside a small image that every SM keeps in L1 — the rate of the
- *          gather pipes themselves, an upper bound for any access pattern.
+ *          gather pipes themselves for this lane spacing.
  * Both run on every SM with enough warps to saturate it and are timed with
  * CUDA events on the caller's stream.
  */
@@ -56,40 +59,45 @@ __global__ void __launch_bounds__(256) gatherProbe(const void *img, int pitch, i
 {
   const int lane = threadIdx.x & 31;
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  /* columns 1.25 px apart across the warp, as adjacent voxels project */
-  const uint32_t span = (uint32_t)(pitch - 64) * (uint32_t)(rows - 2);
+  /* bases in the first (pitch - 64) x (rows - 8) pixels: the lanes' columns
+     (up to 38 px right) and the four fetches' rows (up to 7 rows down, with
+     the lower taps) stay inside the image */
+  const uint32_t span = (uint32_t)(pitch - 64) * (uint32_t)(rows - 8);
   uint32_t state = 2654435761u * (uint32_t)(warp + 1);
   float acc = 0.0f;
   for (int i = 0; i < iters; ++i) {
     state = state * 1664525u + 1013904223u;
-    const uint32_t base = (state >> 8) % span;
-    const uint32_t idx = base + ((uint32_t)lane * 5u >> 2);
-    if (KIND == 0) {
-      const float *f = static_cast<const float *>(img) + idx;
-      acc += __ldg(f) + __ldg(f + 1) + __ldg(f + pitch) + __ldg(f + pitch + 1);
-    } else if (KIND == 1) {
-      const unsigned short *h = static_cast<const unsigned short *>(img) + idx;
-      acc += __uint_as_float(((uint32_t)__ldg(h) << 16) | __ldg(h + 1)) +
-             __uint_as_float(((uint32_t)__ldg(h + pitch) << 16) | __ldg(h + pitch + 1));
-    } else if (KIND == 2) {
-      const float4 q = __ldg(static_cast<const float4 *>(img) + idx);
-      acc += (q.x + q.y) + (q.z + q.w);
-    } else if (KIND == 3) {
-      const uint2 q = __ldg(static_cast<const uint2 *>(img) + idx);
-      acc += __uint_as_float(q.x) + __uint_as_float(q.y);
-    } else if (KIND == 4) {
-      const float cx = (float)(idx % (uint32_t)pitch) + 1.0f;
-      const float cy = (float)(idx / (uint32_t)pitch) + 1.0f;
-      const float4 g = tex2Dgather<float4>(tex, cx, cy, 0);
-      acc += (g.x + g.y) + (g.z + g.w);
-    } else if (KIND == 5) {
-      const float cx = (float)(idx % (uint32_t)pitch) + 0.5f;
-      const float cy = (float)(idx / (uint32_t)pitch) + 0.5f;
-      const float4 g = tex2D<float4>(tex, cx, cy);
-      acc += (g.x + g.y) + (g.z + g.w);
-    } else {
-      const float4 g = tex1Dfetch<float4>(tex, (int)idx);
-      acc += (g.x + g.y) + (g.z + g.w);
+    const uint32_t base = (state >> 8) % span + ((uint32_t)lane * 5u >> 2);
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      const uint32_t idx = base + (uint32_t)(2 * r * pitch);
+      if (KIND == 0) {
+        const float *f = static_cast<const float *>(img) + idx;
+        acc += __ldg(f) + __ldg(f + 1) + __ldg(f + pitch) + __ldg(f + pitch + 1);
+      } else if (KIND == 1) {
+        const unsigned short *h = static_cast<const unsigned short *>(img) + idx;
+        acc += __uint_as_float(((uint32_t)__ldg(h) << 16) | __ldg(h + 1)) +
+               __uint_as_float(((uint32_t)__ldg(h + pitch) << 16) | __ldg(h + pitch + 1));
+      } else if (KIND == 2) {
+        const float4 q = __ldg(static_cast<const float4 *>(img) + idx);
+        acc += (q.x + q.y) + (q.z + q.w);
+      } else if (KIND == 3) {
+        const uint2 q = __ldg(static_cast<const uint2 *>(img) + idx);
+        acc += __uint_as_float(q.x) + __uint_as_float(q.y);
+      } else if (KIND == 4) {
+        const float cx = (float)(idx % (uint32_t)pitch) + 1.0f;
+        const float cy = (float)(idx / (uint32_t)pitch) + 1.0f;
+        const float4 g = tex2Dgather<float4>(tex, cx, cy, 0);
+        acc += (g.x + g.y) + (g.z + g.w);
+      } else if (KIND == 5) {
+        const float cx = (float)(idx % (uint32_t)pitch) + 0.5f;
+        const float cy = (float)(idx / (uint32_t)pitch) + 0.5f;
+        const float4 g = tex2D<float4>(tex, cx, cy);
+        acc += (g.x + g.y) + (g.z + g.w);
+      } else {
+        const float4 g = tex1Dfetch<float4>(tex, (int)idx);
+        acc += (g.x + g.y) + (g.z + g.w);
+      }
     }
   }
   if (acc == 1234.5f)
@@ -143,13 +151,13 @@ extern "C" double lolaCudaProbeGatherRate(int storage, int width, int height)
   return probeStorage(storage, width, height);
 }
 
-/* The same fetches inside a 112 x 16 image (28 KB of FP32 quads) that stays
+/* The same fetches inside a 112 x 24 image (43 KB of FP32 quads) that stays
  * in every SM's L1: the gather pipes' own rate.  (gatherProbe draws bases in
- * the first (pitch - 64) x (rows - 2) pixels, so with 64 + 48 columns every
- * fetch stays inside the image.) */
+ * the first (pitch - 64) x (rows - 8) pixels, so with 64 + 48 columns and
+ * 8 + 16 rows every fetch stays inside the image.) */
 extern "C" double lolaCudaProbeGatherPeak(int storage)
 {
-  return probeStorage(storage, -112, -16);
+  return probeStorage(storage, -112, -24);
 }
 
 static double probeStorage(int storage, int width, int height)
@@ -235,7 +243,7 @@ static double probeKind(int kind, int elem, int channels, int width, int height)
     }
   }
   const int sms = smCount();
-  const int blocks = sms * 8, threads = 256, iters = 2048;
+  const int blocks = sms * 8, threads = 256, iters = 512;  /* 4 fetches per iteration */
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
@@ -250,7 +258,7 @@ static double probeKind(int kind, int elem, int channels, int width, int height)
     default: gatherProbe<6><<<blocks, threads>>>(img, pitch, rows, it, out, tex); break;
     }
   };
-  launch(64);
+  launch(16);
   cudaEventRecord(e0);
   launch(iters);
   cudaEventRecord(e1);
@@ -265,7 +273,7 @@ static double probeKind(int kind, int elem, int channels, int width, int height)
   cudaFree(out);
   if (cudaGetLastError() != cudaSuccess || ms <= 0.0f)
     return -1.0;
-  return (double)blocks * threads * iters / (ms * 1e-3);
+  return (double)blocks * threads * iters * 4.0 / (ms * 1e-3);
 }
 
 extern "C" int lolaCudaDeviceInfo(int *smCountOut, int *clockKHz, char *name, int nameLen)
