@@ -691,7 +691,10 @@ def run_gpu(args, rank, world, local):
                   "gather": {s: lib.lolaCudaProbeGatherRate(STORAGE_IDS[s], scan.width,
                                                             scan.height) for s in used},
                   "gather_peak": {s: lib.lolaCudaProbeGatherPeak(STORAGE_IDS[s])
-                                  for s in used}}
+                                  for s in used},
+                  # lane fetches/s of 8-lane texture requests over 1, 2 or 8
+                  # detector rows: one data-stage wavefront per row touched
+                  "texture_rows": {str(r): lib.lolaCudaProbeTextureRows(r) for r in (1, 2, 8)}}
 
     clocks = ClockSampler(0)
     head = time_device(args, dist, lib, scan, vs, o, d_images, args.storage, clocks)

@@ -458,6 +458,10 @@ double lolaCudaProbeGatherRate(int storage, int width, int height);
 /* The same fetches inside an image small enough to stay in every SM's L1:
  * the rate of the gather pipes themselves for this lane spacing. */
 double lolaCudaProbeGatherPeak(int storage);
+/* Lane fetches per second of 8-lane texture requests (RGBA16F texels by
+ * index, L1-resident) whose eight texels lie in `rows` detector rows (1, 2, 4
+ * or 8; -1 for another value): what a request that straddles rows costs. */
+double lolaCudaProbeTextureRows(int rows);
 /* SM count, SM clock (kHz) and name of the current device. */
 int lolaCudaDeviceInfo(int *smCount, int *clockKHz, char *name, int nameLen);
 

@@ -190,6 +190,7 @@ _SIGNATURES = [
     ("lolaCudaProbeIssueRate", C.c_double, []),
     ("lolaCudaProbeGatherRate", C.c_double, [C.c_int, C.c_int, C.c_int]),
     ("lolaCudaProbeGatherPeak", C.c_double, [C.c_int]),
+    ("lolaCudaProbeTextureRows", C.c_double, [C.c_int]),
     ("lolaCudaDeviceInfo", C.c_int, [C.POINTER(C.c_int), C.POINTER(C.c_int), C.c_char_p,
                                      C.c_int]),
 ]

@@ -104,6 +104,35 @@ __global__ void __launch_bounds__(256) gatherProbe(const void *img, int pitch, i
     out[0] = acc;
 }
 
+/* 8-lane texture requests whose eight texels lie in `rows` detector rows
+ * (1, 2, 4 or 8): lanes 1.25 px apart within a row, each 8-lane quarter of
+ * the warp 10 px right of the previous one, four independent fetches per
+ * step (8 rows apart), in an L1-resident RGBA16F linear texture of
+ * 128 x 48 texels. */
+__global__ void __launch_bounds__(256) textureRowsProbe(int rows, int iters, float *out,
+    cudaTextureObject_t tex)
+{
+  const int lane = threadIdx.x & 31, q = lane >> 3, j = lane & 7;
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int perRow = 8 / rows;
+  uint32_t state = 2654435761u * (uint32_t)(warp + 1);
+  float acc = 0.0f;
+  for (int i = 0; i < iters; ++i) {
+    state = state * 1664525u + 1013904223u;
+    const int bc = (int)((state >> 8) & 31u), br = (int)((state >> 16) & 7u);
+    /* columns <= 31 + 30 + 8, rows <= 7 + 7 + 24: inside the 128 x 48 image */
+    const int col = bc + q * 10 + ((j % perRow) * 5) / 4;
+    const int row = br + j / perRow;
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      const float4 g = tex1Dfetch<float4>(tex, (row + 8 * r) * 128 + col);
+      acc += (g.x + g.y) + (g.z + g.w);
+    }
+  }
+  if (acc == 1234.5f)
+    out[0] = acc;
+}
+
 int smCount()
 {
   int dev = 0, sms = 0;
@@ -269,6 +298,59 @@ static double probeKind(int kind, int elem, int channels, int width, int height)
   cudaEventDestroy(e1);
   if (tex)
     cudaDestroyTextureObject(tex);
+  cudaFree(img);
+  cudaFree(out);
+  if (cudaGetLastError() != cudaSuccess || ms <= 0.0f)
+    return -1.0;
+  return (double)blocks * threads * iters * 4.0 / (ms * 1e-3);
+}
+
+/* Lane fetches per second of 8-lane texture requests spanning `rows`
+ * detector rows (1, 2, 4 or 8): the texture data stage takes one wavefront
+ * per row (or 128-byte window) that a request touches. */
+extern "C" double lolaCudaProbeTextureRows(int rows)
+{
+  if (rows != 1 && rows != 2 && rows != 4 && rows != 8)
+    return -1.0;
+  const int width = 128, height = 48, elem = 8;
+  const size_t bytes = (size_t)width * height * elem;
+  void *img = nullptr;
+  float *out = nullptr;
+  if (cudaMalloc(&img, bytes) != cudaSuccess)
+    return -1.0;
+  if (cudaMalloc(&out, sizeof(float)) != cudaSuccess) {
+    cudaFree(img);
+    return -1.0;
+  }
+  cudaMemset(img, 0, bytes);
+  cudaResourceDesc rd = {};
+  rd.resType = cudaResourceTypeLinear;
+  rd.res.linear.devPtr = img;
+  rd.res.linear.desc = cudaCreateChannelDesc(16, 16, 16, 16, cudaChannelFormatKindFloat);
+  rd.res.linear.sizeInBytes = bytes;
+  cudaTextureDesc td = {};
+  td.filterMode = cudaFilterModePoint;
+  td.readMode = cudaReadModeElementType;
+  cudaTextureObject_t tex = 0;
+  if (cudaCreateTextureObject(&tex, &rd, &td, nullptr) != cudaSuccess) {
+    cudaFree(img);
+    cudaFree(out);
+    return -1.0;
+  }
+  const int blocks = smCount() * 8, threads = 256, iters = 256;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  textureRowsProbe<<<blocks, threads>>>(rows, 16, out, tex);
+  cudaEventRecord(e0);
+  textureRowsProbe<<<blocks, threads>>>(rows, iters, out, tex);
+  cudaEventRecord(e1);
+  cudaEventSynchronize(e1);
+  float ms = 0.0f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaDestroyTextureObject(tex);
   cudaFree(img);
   cudaFree(out);
   if (cudaGetLastError() != cudaSuccess || ms <= 0.0f)
