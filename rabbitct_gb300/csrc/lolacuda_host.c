@@ -213,6 +213,7 @@ struct LolaCudaPlan {
   cudaEvent_t upChunk[LOLA_XFER_CHUNKS], outChunk[LOLA_XFER_CHUNKS];
   cudaEvent_t xferDone, streamMark;
   int uploadChunks;  /* chunks of an asynchronous upload the next pass waits for */
+  const float *uploadSrc;  /* host volume of an asynchronous upload not yet issued */
   int xferPending;   /* transfers the plan stream is not yet ordered after */
   float *streamOut;  /* host target for the volume after the next pass */
   float *outValid;   /* host copy streamed out after the last pass, if any */
@@ -473,8 +474,45 @@ int lolaCudaPlanCreate(const LolaCudaGeometry *g, const LolaCudaConfig *cfg, Lol
 }
 
 /* Orders the plan stream after every volume transfer issued so far. */
+static void xferChunkRange(const LolaCudaPlan *p, int c, int k, int *zb, int *ze);
+
+/* Issues an asynchronous volume upload that lolaCudaPlanUploadVolumeAsync
+ * deferred: its z-chunk copies on the transfer stream after the plan stream's
+ * work so far, each chunk's landing recorded for the pass that waits for it.
+ * Deferred to the first pass that needs the volume (or any other use of it),
+ * so that pass's projections, copied by the calls before it, do not queue
+ * behind the whole volume on the host link: in the module API the first pass
+ * then starts on chunk 0 about 3 ms after its projections are in, instead of
+ * after the entire 4 GiB upload (24 ms at N=1024). */
+static int issueUpload(LolaCudaPlan *p)
+{
+  if (p->uploadSrc == NULL)
+    return 1;
+  const float *h = p->uploadSrc;
+  p->uploadSrc = NULL;
+  cudaStream_t us = p->xferStream;
+  /* the upload overwrites what earlier work on the plan stream produces */
+  CUDA_TRY(cudaEventRecord(p->streamMark, p->stream));
+  CUDA_TRY(cudaStreamWaitEvent(us, p->streamMark, 0));
+  const int k = p->uploadChunks;
+  const size_t slice = (size_t)p->geom.problemSize * (size_t)p->geom.problemSize;
+  for (int c = 0; c < k; c++) {
+    int zb, ze;
+    xferChunkRange(p, c, k, &zb, &ze);
+    if (ze > zb)
+      CUDA_TRY(cudaMemcpyAsync(p->d_volume + (size_t)zb * slice, h + (size_t)zb * slice,
+          (size_t)(ze - zb) * slice * sizeof(float), cudaMemcpyHostToDevice, us));
+    CUDA_TRY(cudaEventRecord(p->upChunk[c], us));
+  }
+  CUDA_TRY(cudaEventRecord(p->xferDone, us));
+  p->xferPending = 1;
+  return 1;
+}
+
 static int joinTransfers(LolaCudaPlan *p)
 {
+  if (!issueUpload(p))
+    return 0;
   if (p->xferPending) {
     CUDA_TRY(cudaStreamWaitEvent(p->stream, p->xferDone, 0));
     p->xferPending = 0;
@@ -583,22 +621,9 @@ int lolaCudaPlanUploadVolumeAsync(LolaCudaPlan *p, const float *h)
   if (p == NULL || h == NULL)
     return setError("null argument");
   CUDA_TRY(cudaSetDevice(p->device));
-  /* the upload overwrites what earlier work on the plan stream produces */
-  CUDA_TRY(cudaEventRecord(p->streamMark, p->stream));
-  CUDA_TRY(cudaStreamWaitEvent(p->xferStream, p->streamMark, 0));
-  const int k = xferChunks(p);
-  const size_t slice = (size_t)p->geom.problemSize * (size_t)p->geom.problemSize;
-  for (int c = 0; c < k; c++) {
-    int zb, ze;
-    xferChunkRange(p, c, k, &zb, &ze);
-    if (ze > zb)
-      CUDA_TRY(cudaMemcpyAsync(p->d_volume + (size_t)zb * slice, h + (size_t)zb * slice,
-          (size_t)(ze - zb) * slice * sizeof(float), cudaMemcpyHostToDevice, p->xferStream));
-    CUDA_TRY(cudaEventRecord(p->upChunk[c], p->xferStream));
-  }
-  CUDA_TRY(cudaEventRecord(p->xferDone, p->xferStream));
-  p->xferPending = 1;
-  p->uploadChunks = k;
+  /* a previous upload not yet issued is overwritten by this one anyway */
+  p->uploadSrc = h;
+  p->uploadChunks = xferChunks(p);
   p->outValid = NULL;
   return 1;
 }
@@ -866,6 +891,8 @@ static int launchPass(LolaCudaPlan *p, const double *mats, int count)
   } else {
     /* chunk by chunk: each starts once its slices have landed and/or is
        copied out as soon as it is done; tiles are those of a whole pass */
+    if (up && !issueUpload(p))
+      return 0;
     if (!up && !joinTransfers(p))
       return 0;
     const int k = up ? p->uploadChunks : xferChunks(p);
@@ -1063,6 +1090,8 @@ int lolaCudaPlanSynchronize(LolaCudaPlan *p)
     return setError("null plan");
   CUDA_TRY(cudaSetDevice(p->device));
   if (!flushPending(p))
+    return 0;
+  if (!issueUpload(p))
     return 0;
   if (p->streamOut != NULL) {
     /* no pass consumed the stream-out request: copy the volume as it is */
@@ -1277,9 +1306,9 @@ int lolaCudaPrepare(RabbitCtGlobalData *d)
   if (!lolaCudaPlanCreate(&g, &c, &gPlan))
     return moduleFail("prepare");
   /* the module accumulates into whatever the caller's volume holds, like
-     LolaBunny's `+=` (src/LolaBunny.c:68); the upload runs on while the first
-     batch is staged, and the first pass starts on each z-chunk as it lands
-     (the runner leaves volumeData alone until finish) */
+     LolaBunny's `+=` (src/LolaBunny.c:68); the upload is issued with the
+     first pass, after the projections it reads, and that pass starts on each
+     z-chunk as it lands (the runner leaves volumeData alone until finish) */
   if (!lolaCudaPlanUploadVolumeAsync(gPlan, d->volumeData))
     return moduleFail("prepare");
   gTotalProjections = d->numberOfProjections;
