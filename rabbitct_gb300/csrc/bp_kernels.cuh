@@ -741,11 +741,11 @@ __device__ __forceinline__ void applyPairs(const TileProj &tp, const void *img,
  * differ (the magnification then moves them up to about a pixel per 8
  * voxels at the detector's top and bottom), so GROUPS gives each quarter a
  * 4 x 2 patch instead of a row of 8 voxels: its depth spread is
- * 3|sin a| + |cos a| voxels instead of 7|sin a| over the ray angle a, and
- * it straddles a row boundary about half as often (f16qx at N=1024: 1.63
- * wavefronts per quarter with rows of 8; 1775 -> 1868 GUPS with 4 x 2
- * quarters, bit-identical volumes).  Without GROUPS the warp's lanes run
- * along x row by row. */
+ * 3|sin a| + |cos a| voxels instead of 7|sin a| (a: the angle between the
+ * ray and the y axis), and it straddles a row boundary about half as often
+ * (f16qx: 1.63 -> 1.47 wavefronts per quarter at N=640, 1775 -> 1868 GUPS
+ * at N=1024, bit-identical volumes; lolaStorePitch's row skew then takes it
+ * to 1.19).  Without GROUPS the warp's lanes run along x row by row. */
 #ifndef LOLA_LANE_GROUPS
 #define LOLA_LANE_GROUPS -1  /* -1: per storage (LaneGroups); 0: never; 1: always */
 #endif
