@@ -95,8 +95,10 @@ class Plan:
         check(self.lib.lolaCudaPlanUploadVolume(self.handle, vol.ctypes.data), "upload volume")
 
     def upload_async(self, vol: np.ndarray) -> None:
-        """Starts a chunked upload that the next pass overlaps; `vol` is kept
-        alive (and must stay unchanged) until synchronize()."""
+        """A chunked upload that the next pass overlaps: its copies are issued
+        with that pass, after the projections it reads (or by any other use
+        of the volume, or synchronize()); `vol` is kept alive (and must stay
+        unchanged) until synchronize()."""
         assert vol.dtype == np.float32 and vol.flags.c_contiguous
         assert vol.size == self.n * self.n * self.slab[1]
         self._hold.append(vol)
