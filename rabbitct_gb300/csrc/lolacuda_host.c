@@ -473,7 +473,6 @@ int lolaCudaPlanCreate(const LolaCudaGeometry *g, const LolaCudaConfig *cfg, Lol
   return 1;
 }
 
-/* Orders the plan stream after every volume transfer issued so far. */
 static void xferChunkRange(const LolaCudaPlan *p, int c, int k, int *zb, int *ze);
 
 /* Issues an asynchronous volume upload that lolaCudaPlanUploadVolumeAsync
@@ -509,6 +508,8 @@ static int issueUpload(LolaCudaPlan *p)
   return 1;
 }
 
+/* Orders the plan stream after every volume transfer, issuing a deferred
+   upload first. */
 static int joinTransfers(LolaCudaPlan *p)
 {
   if (!issueUpload(p))
