@@ -206,14 +206,15 @@ int lolaCudaPlanZeroVolume(LolaCudaPlan *plan);
 /* Synchronous copies of the whole volume. */
 int lolaCudaPlanUploadVolume(LolaCudaPlan *plan, const float *h_volume);
 int lolaCudaPlanDownloadVolume(LolaCudaPlan *plan, float *h_volume);
-/* Uploads h_volume asynchronously in z-chunks on the plan's transfer stream
- * and returns at once.  The copies are issued with the next pass, after the
- * projections that pass reads (or by any other operation on the volume or
- * lolaCudaPlanSynchronize, whichever comes first), and that pass starts on
- * each chunk as soon as it has landed.  h_volume must stay unchanged until
- * lolaCudaPlanSynchronize (page-locked memory lets the copies run without
- * holding the host).  The next host-staged pass takes up to the edge batch
- * of projections (LolaCudaConfig.edgeBatch). */
+/* Uploads h_volume asynchronously in z-chunks on the plan's transfer stream;
+ * the next pass starts on each chunk as soon as it has landed.  From
+ * page-locked memory the call returns at once and the copies are issued with
+ * that pass, after the projections it reads (or by any other operation on
+ * the volume or lolaCudaPlanSynchronize, whichever comes first); from
+ * pageable memory they are issued before the call returns (the driver holds
+ * the thread until it has read the volume).  h_volume must stay unchanged
+ * until lolaCudaPlanSynchronize.  The next host-staged pass takes up to the
+ * edge batch of projections (LolaCudaConfig.edgeBatch). */
 int lolaCudaPlanUploadVolumeAsync(LolaCudaPlan *plan, const float *h_volume);
 /* Asks for the volume in h_volume after the last pass of the next
  * backprojection call (lolaCudaPlanBackprojectHost / Device): that pass runs

@@ -626,6 +626,16 @@ int lolaCudaPlanUploadVolumeAsync(LolaCudaPlan *p, const float *h)
   p->uploadSrc = h;
   p->uploadChunks = xferChunks(p);
   p->outValid = NULL;
+  /* from page-locked memory the copies wait for the next pass; from pageable
+     memory the driver stages them through its own buffers and holds this
+     thread until it has read the volume, so they are issued here, where the
+     module API's prepare pays for them, as before */
+  struct cudaPointerAttributes attr;
+  const int pinned = cudaPointerGetAttributes(&attr, h) == cudaSuccess &&
+                     attr.type == cudaMemoryTypeHost;
+  cudaGetLastError(); /* an unknown pointer is not an error here */
+  if (!pinned)
+    return issueUpload(p);
   return 1;
 }
 

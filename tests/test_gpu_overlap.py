@@ -210,22 +210,43 @@ def test_module_api_overlap_matches_plan(lib, scan7, with_geometry, pinned, edge
             lib.lolaCudaHostFree(host)
 
 
-def test_deferred_upload_reaches_the_volume_without_a_pass(lib):
-    """The asynchronous upload is issued with the next pass; with none, by
-    synchronize or by any other use of the volume.  A second upload before
+@pytest.mark.parametrize("pinned", [True, False])
+def test_deferred_upload_reaches_the_volume_without_a_pass(lib, pinned):
+    """From page-locked memory the asynchronous upload is issued with the
+    next pass; with none, by synchronize or by any other use of the volume
+    (from pageable memory it is issued at once).  A second upload before
     either replaces the first."""
+    import ctypes as C
+
     from rabbitct_gb300.lolacuda import Plan
     vs, o = _geom(64)
-    a, b = _initial(64, 64, seed=11), _initial(64, 64, seed=12)
-    with Plan(64, vs, o, 96, 80, batch=4) as p:
-        p.upload_async(a)
-        p.synchronize()
-        assert np.array_equal(p.download(), a)
-        p.upload_async(a)
-        p.upload_async(b)
-        assert np.array_equal(p.download(), b)   # download issues it first
-        p.upload_async(a)
-        out = np.full_like(a, np.nan)
-        p.stream_out(out)                        # no pass: copied at synchronize
-        p.synchronize()
-        assert np.array_equal(out, a)
+    shape, nbytes = (64, 64, 64), 4 * 64 ** 3
+    bufs = []
+
+    def host_array():
+        if not pinned:
+            return np.empty(shape, np.float32)
+        ptr = lib.lolaCudaHostAlloc(nbytes)
+        assert ptr
+        bufs.append(ptr)
+        return np.ctypeslib.as_array((C.c_float * (nbytes // 4)).from_address(ptr)).reshape(shape)
+
+    try:
+        a, b, out = host_array(), host_array(), host_array()
+        a[...] = _initial(64, 64, seed=11)
+        b[...] = _initial(64, 64, seed=12)
+        with Plan(64, vs, o, 96, 80, batch=4) as p:
+            p.upload_async(a)
+            p.synchronize()
+            assert np.array_equal(p.download(), a)
+            p.upload_async(a)
+            p.upload_async(b)
+            assert np.array_equal(p.download(), b)   # download issues it first
+            p.upload_async(a)
+            out[...] = np.nan
+            p.stream_out(out)                        # no pass: copied at synchronize
+            p.synchronize()
+            assert np.array_equal(out, a)
+    finally:
+        for ptr in bufs:
+            lib.lolaCudaHostFree(ptr)
