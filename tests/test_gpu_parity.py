@@ -188,10 +188,10 @@ def test_fp32_quads_equal_plain_fp32(lib, storage):
 
 @pytest.mark.parametrize("n", [128, 640])
 def test_mixed_fp16_quads_equal_load_only_quads(lib, n):
-    """f16qx (column-ordered quads, some voxels through the texture unit: 8
-    of 16 up to N=512, 10 of 16 above) and f16q (row-ordered quads, loads
-    only) hold the same FP16 terms, and the texture's point fetch widens them
-    exactly: the volumes are identical on either side of the mask switch."""
+    """f16qx (column-ordered quads, every voxel through the texture unit,
+    4 x 2 voxels per warp quarter) and f16q (row-ordered quads, loads only,
+    rows of 8 lanes) hold the same FP16 terms, and the texture's point fetch
+    widens them exactly: the volumes are identical."""
     from rabbitct_gb300.lolacuda import Plan
     spec = synth.ScanSpec(nproj=4, seed=4)
     scan = synth.make_scan(spec)
