@@ -503,6 +503,13 @@ def roofline(args, lib, storage, st, probes, cfg=None) -> dict:
     pipes = pipe_utilisation(storage)
     if pipes is not None:
         ceil["ncu_pipes"] = pipes
+        wpr = pipes.get("tex_wf_per_request")
+        if probes and isinstance(wpr, float) and wpr > 0:
+            # the texture pipe's rate for the kernel's own access pattern: the
+            # probe's requests take one data-stage wavefront each, the kernel's
+            # wpr on average (detector rows straddled)
+            ceil["peak_gather_locality"] = ceil["peak_gather"] / wpr
+            ceil["frac_of_locality_gather"] = achieved / ceil["peak_gather_locality"]
     out["ceiling"] = ceil
     return out
 

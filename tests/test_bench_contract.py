@@ -62,6 +62,12 @@ def test_roofline_shape(bench):
     assert c["peak"] == pytest.approx(min(c["peak_gather"], c["peak_issue"]))
     assert c["peak_gather"] >= c["gather_l2_random"]
     assert 0 < c["paired_fraction"] <= 1
+    # the committed f16qx capture gives the kernel's wavefronts per texture
+    # request: the locality-matched gather ceiling is the probe's rate over it
+    wpr = c["ncu_pipes"]["tex_wf_per_request"]
+    assert wpr >= 1.0
+    assert c["peak_gather_locality"] == pytest.approx(c["peak_gather"] / wpr)
+    assert c["frac_of_locality_gather"] == pytest.approx(c["achieved"] / c["peak_gather_locality"])
 
 
 def test_traffic_only_for_captured_configurations(bench):
