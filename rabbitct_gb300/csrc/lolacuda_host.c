@@ -213,8 +213,7 @@ struct LolaCudaPlan {
   cudaEvent_t upChunk[LOLA_XFER_CHUNKS], outChunk[LOLA_XFER_CHUNKS];
   cudaEvent_t xferDone, streamMark;
   int uploadChunks;  /* chunks of an asynchronous upload the next pass waits for */
-  const float *uploadSrc;  /* host volume of an asynchronous upload not yet all issued */
-  int uploadIssued;        /* its z-chunks already issued */
+  const float *uploadSrc;  /* host volume of an asynchronous upload not yet issued */
   int xferPending;   /* transfers the plan stream is not yet ordered after */
   float *streamOut;  /* host target for the volume after the next pass */
   float *outValid;   /* host copy streamed out after the last pass, if any */
@@ -476,31 +475,27 @@ int lolaCudaPlanCreate(const LolaCudaGeometry *g, const LolaCudaConfig *cfg, Lol
 
 static void xferChunkRange(const LolaCudaPlan *p, int c, int k, int *zb, int *ze);
 
-/* Issues the z-chunk copies [uploadIssued, upTo) of an asynchronous volume
- * upload on the transfer stream, each chunk's landing recorded for the pass
- * that waits for it, the first after the plan stream's work so far.  From
- * page-locked memory lolaCudaPlanUploadVolumeAsync issues chunk 0 at once and
- * defers the rest to the first pass that needs the volume (or any other use
- * of it), so that pass's projections, copied by the calls before it, queue
- * behind one chunk instead of the whole volume on the host link: in the
- * module API the first pass starts on chunk 0 as soon as its projections are
- * in, instead of after the entire 4 GiB upload (24 ms at N=1024). */
-static int issueUpload(LolaCudaPlan *p, int upTo)
+/* Issues an asynchronous volume upload that lolaCudaPlanUploadVolumeAsync
+ * deferred: its z-chunk copies on the transfer stream after the plan stream's
+ * work so far, each chunk's landing recorded for the pass that waits for it.
+ * Deferred to the first pass that needs the volume (or any other use of it),
+ * so that pass's projections, copied by the calls before it, do not queue
+ * behind the whole volume on the host link: in the module API the first pass
+ * then starts on chunk 0 about 3 ms after its projections are in, instead of
+ * after the entire 4 GiB upload (24 ms at N=1024). */
+static int issueUpload(LolaCudaPlan *p)
 {
   if (p->uploadSrc == NULL)
     return 1;
   const float *h = p->uploadSrc;
-  const int k = p->uploadChunks;
-  if (upTo > k)
-    upTo = k;
+  p->uploadSrc = NULL;
   cudaStream_t us = p->xferStream;
-  if (p->uploadIssued == 0) {
-    /* the upload overwrites what earlier work on the plan stream produces */
-    CUDA_TRY(cudaEventRecord(p->streamMark, p->stream));
-    CUDA_TRY(cudaStreamWaitEvent(us, p->streamMark, 0));
-  }
+  /* the upload overwrites what earlier work on the plan stream produces */
+  CUDA_TRY(cudaEventRecord(p->streamMark, p->stream));
+  CUDA_TRY(cudaStreamWaitEvent(us, p->streamMark, 0));
+  const int k = p->uploadChunks;
   const size_t slice = (size_t)p->geom.problemSize * (size_t)p->geom.problemSize;
-  for (int c = p->uploadIssued; c < upTo; c++) {
+  for (int c = 0; c < k; c++) {
     int zb, ze;
     xferChunkRange(p, c, k, &zb, &ze);
     if (ze > zb)
@@ -508,13 +503,8 @@ static int issueUpload(LolaCudaPlan *p, int upTo)
           (size_t)(ze - zb) * slice * sizeof(float), cudaMemcpyHostToDevice, us));
     CUDA_TRY(cudaEventRecord(p->upChunk[c], us));
   }
-  if (upTo > p->uploadIssued)
-    p->uploadIssued = upTo;
-  if (p->uploadIssued == k) {
-    CUDA_TRY(cudaEventRecord(p->xferDone, us));
-    p->xferPending = 1;
-    p->uploadSrc = NULL;
-  }
+  CUDA_TRY(cudaEventRecord(p->xferDone, us));
+  p->xferPending = 1;
   return 1;
 }
 
@@ -522,7 +512,7 @@ static int issueUpload(LolaCudaPlan *p, int upTo)
    upload first. */
 static int joinTransfers(LolaCudaPlan *p)
 {
-  if (!issueUpload(p, LOLA_XFER_CHUNKS))
+  if (!issueUpload(p))
     return 0;
   if (p->xferPending) {
     CUDA_TRY(cudaStreamWaitEvent(p->stream, p->xferDone, 0));
@@ -632,22 +622,21 @@ int lolaCudaPlanUploadVolumeAsync(LolaCudaPlan *p, const float *h)
   if (p == NULL || h == NULL)
     return setError("null argument");
   CUDA_TRY(cudaSetDevice(p->device));
-  /* the rest of an earlier upload not yet issued is dropped: no pass has
-     waited for it, and this one overwrites the whole volume after any of its
-     chunks already on the transfer stream */
+  /* a previous upload not yet issued is overwritten by this one anyway */
   p->uploadSrc = h;
-  p->uploadIssued = 0;
   p->uploadChunks = xferChunks(p);
   p->outValid = NULL;
-  /* from page-locked memory chunk 0 goes now and the rest with the next
-     pass; from pageable memory the driver stages the copies through its own
-     buffers and holds this thread until it has read the volume, so all of
-     them are issued here, where the module API's prepare pays for them */
+  /* from page-locked memory the copies wait for the next pass; from pageable
+     memory the driver stages them through its own buffers and holds this
+     thread until it has read the volume, so they are issued here, where the
+     module API's prepare pays for them, as before */
   struct cudaPointerAttributes attr;
   const int pinned = cudaPointerGetAttributes(&attr, h) == cudaSuccess &&
                      attr.type == cudaMemoryTypeHost;
   cudaGetLastError(); /* an unknown pointer is not an error here */
-  return issueUpload(p, pinned ? 1 : LOLA_XFER_CHUNKS);
+  if (!pinned)
+    return issueUpload(p);
+  return 1;
 }
 
 int lolaCudaPlanStreamVolumeOut(LolaCudaPlan *p, float *h)
@@ -913,7 +902,7 @@ static int launchPass(LolaCudaPlan *p, const double *mats, int count)
   } else {
     /* chunk by chunk: each starts once its slices have landed and/or is
        copied out as soon as it is done; tiles are those of a whole pass */
-    if (up && !issueUpload(p, LOLA_XFER_CHUNKS))
+    if (up && !issueUpload(p))
       return 0;
     if (!up && !joinTransfers(p))
       return 0;
@@ -1113,7 +1102,7 @@ int lolaCudaPlanSynchronize(LolaCudaPlan *p)
   CUDA_TRY(cudaSetDevice(p->device));
   if (!flushPending(p))
     return 0;
-  if (!issueUpload(p, LOLA_XFER_CHUNKS))
+  if (!issueUpload(p))
     return 0;
   if (p->streamOut != NULL) {
     /* no pass consumed the stream-out request: copy the volume as it is */
