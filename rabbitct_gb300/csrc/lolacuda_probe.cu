@@ -16,7 +16,11 @@
  *          L2-resident projection (no reuse in L1), lolaCudaProbeGatherPeak
  *          inside a small image that every SM keeps in L1 — the rate of the
  *          gather pipes themselves for this lane spacing.
- * Both run on every SM with enough warps to saturate it and are timed with
+ *  texture rows  8-lane texture requests whose texels lie in 1, 2, 4 or 8
+ *          detector rows (lolaCudaProbeTextureRows): the texture data stage
+ *          takes one wavefront per row a request touches, which is why the
+ *          pass kernel gives each warp quarter a compact 4 x 2 voxel patch.
+ * They run on every SM with enough warps to saturate it and are timed with
  * CUDA events on the caller's stream.
  */
 #include <cuda_fp16.h>
