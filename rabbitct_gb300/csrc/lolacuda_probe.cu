@@ -21,7 +21,7 @@
  *          takes one wavefront per row a request touches, which is why the
  *          pass kernel gives each warp quarter a compact 4 x 2 voxel patch.
  * They run on every SM with enough warps to saturate it and are timed with
- * CUDA events on the caller's stream.
+ * CUDA events on the default stream.
  */
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
