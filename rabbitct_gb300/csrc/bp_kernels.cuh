@@ -13,7 +13,9 @@
  * GB300 mapping:
  *  - A CTA of ROWS warps owns a tile of 32 ROWS x VPT voxels: each warp an
  *    LOLA_WARP_X x (32 / LOLA_WARP_X) patch of the xy plane (8 x 4 by default,
- *    a compact detector footprint), each thread VPT voxels along z.  Each
+ *    a compact detector footprint; for the texture-fetched FP16 quads and the
+ *    FP32 quads each 8-lane quarter a 4 x 2 part of it, laneVoxel), each
+ *    thread VPT voxels along z.  Each
  *    thread keeps its VPT voxels (one xy column, consecutive z) in registers for a
  *    whole pass of up to LOLA_MAX_BATCH projections, so the volume crosses HBM
  *    once per pass instead of once per projection.
